@@ -1,0 +1,157 @@
+"""The CPU oracle pinned against the reference.
+
+Three kinds of pin:
+  * the known-answer values NEMO publishes for this path (bsf fingerprints,
+    bench12's interaction count, the man-page log table),
+  * fixtures made by the reference's own load.c / grav.c (tests/golden/*.npz,
+    written by tests/golden/make_golden.py), and
+  * where the NEMO sources are present, the reference libraries themselves.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PINS = json.load(open(os.path.join(HERE, "golden", "reference_pins.json")))
+
+
+def bsf_text(values):
+    s1 = s2 = 0.0
+    for v in values:
+        s1 += v
+        s2 += v * v
+    n = len(values)
+    mean = s1 / n
+    var = s2 / n - mean * mean
+    sig = 0.0 if var <= 0 else var ** 0.5
+    return "%g %g %g %g %d" % (mean, sig, min(values), max(values), n)
+
+
+def test_ran3_matches_reference_sequence(oracle_lib):
+    O = oracle_lib
+    if not O.Reference.available():
+        pytest.skip("reference sources not present")
+    R = O.Reference.get(True)
+    assert np.array_equal(O.ran3_sequence(123, 2000), R.ran3_sequence(123, 2000))
+    assert np.array_equal(O.ran3_sequence(7, 500), R.ran3_sequence(7, 500))
+
+
+@pytest.mark.parametrize("n,key", [(10, "mkplummer_testfile_bsf"), (10240, "nemobench_p0_bsf")])
+def test_mkplummer_bsf(oracle_lib, n, key):
+    m, ph = oracle_lib.mkplummer(n, 123)
+    vals = [0.0] + list(m) + list(ph.ravel())     # Time, Mass, PhaseSpace
+    assert bsf_text(vals) == PINS[key]["value"]
+
+
+def test_hackcode1_testfile_bsf_and_manpage(oracle_lib):
+    O = oracle_lib
+    m, ph = O.make_testdata(128, 123)
+    _, _, _, rows, bsf, _ = O.hackcode1(m, ph)
+    assert bsf.text() == PINS["hackcode1_testfile_bsf"]["value"]
+    for row, key in ((rows[0], "manpage_first"), (rows[-1], "manpage_last")):
+        pin = PINS[key]
+        assert "%.3f" % row.tnow == "%.3f" % pin["tnow"]
+        assert "%.4f" % row.etot[0] == "%.4f" % pin["T+U"]
+        assert "%.4f" % (row.etot[1] / row.etot[2]) == "%.4f" % pin["T/U"]
+        assert (row.nttot, row.nbavg, row.ncavg) == (pin["nttot"], pin["nbavg"], pin["ncavg"])
+        for k in range(3):
+            assert "%.4f" % row.cmphase[k] == "%.4f" % pin["cmpos"][k]
+            assert "%.4f" % row.cmphase[3 + k] == "%.4f" % pin["cmvel"][k]
+
+
+def test_nemobench_h0_bsf(oracle_lib):
+    m, ph = oracle_lib.make_testdata(10240, 123)
+    _, _, _, _, bsf, _ = oracle_lib.hackcode1(m, ph)
+    assert bsf.text() == PINS["nemobench_h0_bsf"]["value"]
+
+
+@pytest.mark.slow
+def test_bench12_interaction_count(oracle_lib):
+    m, ph = oracle_lib.mkplummer(200000, 123)
+    _, _, _, rows, _, _ = oracle_lib.hackcode1(m, ph, eps=0.05, tstop=0.125, freq=128, write_out=False)
+    r = rows[-1]
+    pin = PINS["bench12_line"]
+    assert r.nttot == pin["nttot"]
+    assert (r.nbavg, r.ncavg) == (pin["nbavg"], pin["ncavg"])
+    assert "%.4f" % r.etot[0] == "%.4f" % pin["T+U"]
+    assert "%.4f" % (r.etot[1] / r.etot[2]) == "%.4f" % pin["T/U"]
+
+
+def _canon(d):
+    k = np.lexsort((d["corner"][:, 2], d["corner"][:, 1], d["corner"][:, 0], d["level"]))
+    return {f: d[f][k] for f in ("level", "corner", "count", "mass", "cm", "quad")}
+
+
+@pytest.mark.parametrize("case", ["plummer4096_s123", "testdata128_s123", "plummer2048_s7_test"])
+@pytest.mark.parametrize("quad", [False, True])
+def test_oracle_bit_exact_vs_reference_fixture(oracle_lib, case, quad):
+    O = oracle_lib
+    g = np.load(os.path.join(HERE, "golden", case + ".npz"))
+    tag = "qp" if quad else "mp"
+    m, pos = g["mass"], g["pos"]
+    T = O.Tree(len(m), 1.0)
+    assert T.build(m, pos, quad) == 0
+    rmin, rsize = T.box()
+    assert np.array_equal(rmin, g[f"{tag}_rmin"]) and rsize == float(g[f"{tag}_rsize"])
+    c = _canon(T.dump())
+    for f in ("level", "corner", "count", "mass", "cm", "quad"):
+        assert np.array_equal(c[f], g[f"{tag}_cell_{f}"]), f
+    assert np.array_equal(T.dump()["body_parent_level"], g[f"{tag}_body_parent_level"])
+    tp = g["test_pos"] if "test_pos" in g.files else None
+    acc, phi, n2b, nbc = T.forces(float(g["tol"]), float(g["eps"]), quad, test_pos=tp)
+    assert np.array_equal(acc, g[f"{tag}_acc"])
+    assert np.array_equal(phi, g[f"{tag}_phi"])
+    assert np.array_equal(n2b, g[f"{tag}_n2b"]) and np.array_equal(nbc, g[f"{tag}_nbc"])
+
+
+def test_oracle_vs_live_reference_expansion_chain(oracle_lib):
+    """Second massive body far away: expandbox grafts a chain of one-body
+    cells (load.c:74-93); the oracle must reproduce that cell set."""
+    O = oracle_lib
+    if not O.Reference.available():
+        pytest.skip("reference sources not present")
+    far = np.array([[0.1, 0.2, 0.3], [40.0, -70.0, 15.0], [45.0, -65.0, 18.0], [38.0, -71.0, 12.0]])
+    m4 = np.full(4, 0.25)
+    m, ph = O.mkplummer(300, 5)
+    pos = ph[:, 0].copy()
+    pos[1] = [40.0, -70.0, 15.0]
+    for masses, posn, lone in ((m4, far, True), (m, pos, False)):
+        for quad in (False, True):
+            R = O.Reference.get(quad)
+            R.build(masses, posn)
+            T = O.Tree(len(masses), 4.0)
+            assert T.build(masses, posn, quad) == 0
+            a, b = _canon(T.dump()), _canon(R.dump())
+            for f in a:
+                assert np.array_equal(a[f], b[f]), f
+            assert (b["count"] == 1).any() == lone
+            r1 = T.forces(0.6, 0.02, quad)
+            r2 = R.forces(0.6, 0.02)
+            for x, y in zip(r1, r2):
+                assert np.array_equal(x, y)
+
+
+def test_oracle_direct_sum_is_tol0_walk(oracle_lib):
+    O = oracle_lib
+    m, ph = O.mkplummer(512, 3)
+    pos = ph[:, 0].copy()
+    T = O.Tree(512)
+    T.build(m, pos)
+    acc_t, phi_t, _, _ = T.forces(0.0, 0.05)
+    acc_d, phi_d = O.direct(m, pos, eps=0.05)
+    assert np.allclose(acc_t, acc_d, rtol=1e-12, atol=1e-14)
+    assert np.allclose(phi_t, phi_d, rtol=1e-12)
+
+
+def test_oracle_errors(oracle_lib):
+    O = oracle_lib
+    m, ph = O.mkplummer(256, 9)
+    pos = ph[:, 0].copy()
+    T = O.Tree(256, 0.1)                 # fcells too small -> makecell error
+    assert T.build(m, pos) == 1
+    pos2 = pos.copy()
+    pos2[3] = pos2[7]                    # coincident -> assert(l != 0)
+    T2 = O.Tree(256, 1.0)
+    assert T2.build(m, pos2) == 2
