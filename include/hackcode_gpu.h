@@ -1,0 +1,164 @@
+/*
+ * hackcode_gpu.h -- C ABI of the GB300 hackcode1 treecode library
+ * (nemo_gb300/libhackcode_gpu.so).
+ *
+ * NEMO has no plugin interface for force solvers: the reference's "operator
+ * API" for this path is the hackcode1 / hackforce programs themselves
+ * (src/nbody/evolve/hackcode/hackcode1/code.c:21-51 keywords,
+ * hackforce.c:38-50).  This header is the thin C layer those programs (and the
+ * ctypes mirror in nemo_gb300/hackcode.py) call.  Each entry point names the
+ * reference routine it replaces.
+ *
+ * Conventions: plain C types only; every function returns HC_OK (0) or a
+ * negative HC_ERR_* code and never exits; hc_last_error() gives the message.
+ * Host arrays are FP64 in the reference's layouts (Mass[n],
+ * PhaseSpace[n][2][3], Acceleration[n][3], Potential[n]).  One context owns
+ * one CUDA stream and all device memory for one system; one host thread
+ * drives a context at a time.
+ */
+#ifndef HACKCODE_GPU_H
+#define HACKCODE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    HC_OK = 0,
+    HC_ERR_ARG = -1,        /* bad argument */
+    HC_ERR_CUDA = -2,       /* CUDA runtime error */
+    HC_ERR_CELLS = -3,      /* more than fcells*nbody cells needed (load.c:237-239) */
+    HC_ERR_COINCIDENT = -4, /* two massive bodies share integer coords (load.c:113) */
+    HC_ERR_STACK = -5,      /* walk traversal stack exhausted */
+    HC_ERR_STATE = -6,      /* call out of order (e.g. forces before tree) */
+    HC_ERR_NOMEM = -7       /* device allocation failed */
+};
+
+typedef struct hc_ctx hc_ctx;
+
+/* Run parameters (hackcode1 keywords tol= eps= fcells= and usequad=, the
+ * switch between the hackcode1 and hackcode1_qp builds,
+ * hackcode1/Makefile:99-115). */
+typedef struct {
+    double tol;      /* cell-opening tolerance, grav.c:122-131 (tol=0: direct sum) */
+    double eps;      /* Plummer softening, grav.c:42-73 */
+    double fcells;   /* cell pool = fcells * nbody (load.c:49-53) */
+    int usequad;     /* 1: quadrupole moments (QUADPOLE build) */
+    int count_per_body; /* 1: keep per-body interaction counts */
+} hc_params;
+
+/* Diagnostics of code_io.c:160-197 plus interaction totals of the last force
+ * evaluation (64-bit: the reference's int counters wrap at N=1M). */
+typedef struct {
+    double etot[3];      /* T+U, T, U (U = 1/2 sum m phi) */
+    double keten[9];     /* kinetic energy tensor */
+    double peten[9];     /* potential energy tensor sum m x_i a_j */
+    double amten[9];     /* antisymmetric angular momentum tensor */
+    double cmphase[6];   /* centre of mass position, velocity */
+    double mtot;
+    int64_t n2b;         /* body-body interactions */
+    int64_t nbc;         /* body-cell interactions */
+    int64_t nfcalc;      /* force evaluations (bodies walked) */
+} hc_diag;
+
+/* Tree summary (for the structural parity check against maketree). */
+typedef struct {
+    int64_t nbody_massive;
+    int64_t ncell;
+    int32_t max_level;
+    double rmin[3];
+    double rsize;
+} hc_tree_info;
+
+/* Create a context for nbody bodies.  Allocates all device memory once
+ * (the reference allocates its cell pool once too, load.c:49-53).
+ * Replaces: startrun's allocation and box set-up, code.c:70-122. */
+int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params);
+void hc_destroy(hc_ctx *ctx);
+const char *hc_last_error(const hc_ctx *ctx);
+int hc_set_params(hc_ctx *ctx, const hc_params *params);
+
+/* Upload Mass[n] and PhaseSpace[n][2][3] from host memory.
+ * Replaces: inputdata / get_snap body fill, code_io.c:35-56. */
+int hc_upload(hc_ctx *ctx, const double *mass, const double *phase);
+
+/* Root box (rmin, rsize); starts at (-2,-2,-2), 4 (code.c:119-120) and only
+ * grows (expandbox, load.c:68-95). */
+int hc_set_box(hc_ctx *ctx, const double rmin[3], double rsize);
+int hc_get_box(hc_ctx *ctx, double rmin[3], double *rsize);
+
+/* Build the octree of the massive bodies: expandbox replay, 90-bit keys,
+ * radix sort, cell linking, monopole/quadrupole upward pass.
+ * Replaces: maketree + hackcofm, load.c:32-248. */
+int hc_build_tree(hc_ctx *ctx);
+int hc_tree_summary(hc_ctx *ctx, hc_tree_info *info);
+
+/* Cell dump for the structural check (a): per cell its level, integer lower
+ * corner on the 2^30 grid, body count, mass, centre of mass and quadrupole
+ * (xx,xy,xz,yy,yz,zz); per body (original order) its parent cell level or
+ * -1.  Arrays sized by hc_tree_summary().ncell / nbody. */
+int hc_dump_tree(hc_ctx *ctx, int32_t *level, int32_t *corner, int32_t *count, double *mass,
+                 double *cm, double *quad, int32_t *body_parent_level);
+
+/* Forces at every body, its own body skipped (hackgrav for each body,
+ * grav.c:22-32 as looped in code.c:169-180).  Results stay on the device
+ * (hc_download).  Requires hc_build_tree. */
+int hc_forces(hc_ctx *ctx);
+
+/* Forces at ntest separate test points that are not part of the tree
+ * (hackforce test=, hackforce.c:206-213).  test_pos is host [ntest][3];
+ * acc [ntest][3] / phi [ntest] receive the results (host). */
+int hc_forces_at(hc_ctx *ctx, const double *test_pos, int64_t ntest, double *acc, double *phi);
+
+/* Download PhaseSpace / Acceleration / Potential (any may be NULL).
+ * Replaces: the put_snap body gather, code_io.c:147-151. */
+int hc_download(hc_ctx *ctx, double *phase, double *acc, double *phi);
+
+/* Per-body interaction counts of the last hc_forces (original order);
+ * requires params.count_per_body. */
+int hc_body_counts(hc_ctx *ctx, int32_t *n2b, int32_t *nbc);
+
+/* One hackcode1 leapfrog step (stepsystem, code.c:159-191): maketree,
+ * forces with the closing half-kick v += (a_new - a_old) dt/2 when
+ * nstep > 0, diagnostics into *diag (may be NULL), then the kick-drift
+ * v1/2 = v + a dt/2, x += v1/2 dt, v = v1/2 + a dt/2.  The state after the
+ * force evaluation (what output() writes) is captured in *diag and, when
+ * snap_phase/snap_acc/snap_phi are non-NULL, copied to those host arrays
+ * before the drift. */
+int hc_step(hc_ctx *ctx, double dt, int64_t nstep, hc_diag *diag, double *snap_phase,
+            double *snap_acc, double *snap_phi);
+
+/* Diagnostics of the current device state (code_io.c:160-197). */
+int hc_diagnostics(hc_ctx *ctx, hc_diag *diag);
+
+/* FP64 direct-sum accelerations/potentials at nsample bodies (indices into
+ * the original order, self skipped): the exact (tol=0) limit of the walk,
+ * used to state force errors.  Results to host acc [nsample][3], phi. */
+int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t nsample, double *acc, double *phi);
+
+/* Timing of the last hc_build_tree / hc_forces (milliseconds, CUDA events on
+ * the context stream) and kernel launch count of the last call. */
+int hc_last_timing(hc_ctx *ctx, double *build_ms, double *walk_ms, int64_t *launches);
+
+/* Device timers on the context stream (CUDA events): start, then stop
+ * returns the elapsed milliseconds; both bracket whatever was launched on the
+ * context between them. */
+int hc_timer_start(hc_ctx *ctx);
+int hc_timer_stop(hc_ctx *ctx, double *ms);
+
+/* Measured FP32 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops): the
+ * denominator of the walk's roofline fraction. */
+int hc_fp32_peak(hc_ctx *ctx, double *tflops);
+
+/* Initial conditions (host, FP64), drawn with NEMO's xrandom/ran3:
+ * mkplummer with its default keywords (src/nbody/init/mkplummer.c:257-422)
+ * and hackcode1's nbody= test data (hackcode1/code.c:129-153). */
+void hc_mkplummer(int n, int seed, double *mass, double *phase);
+void hc_make_testdata(int n, int seed, int cencon, double *mass, double *phase);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,564 @@
+// hc_api.cu -- the C ABI declared in include/hackcode_gpu.h.
+//
+// Every entry point validates its arguments, launches on the context's own
+// stream, checks the device status word when it synchronises, and returns an
+// HC_* code with the message kept in the context (hc_last_error).  Nothing
+// here exits the process; nothing here falls back to a CPU path.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <vector>
+#include "hc_internal.cuh"
+
+namespace {
+
+template <typename T>
+int dalloc(hc_ctx *c, T **p, int64_t count)
+{
+    size_t bytes = sizeof(T) * (size_t)std::max<int64_t>(count, 1);
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e != cudaSuccess) {
+        c->err = std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+        *p = nullptr;
+        return HC_ERR_NOMEM;
+    }
+    return HC_OK;
+}
+
+#define HC_TRY(x)                  \
+    do {                           \
+        int r_ = (x);              \
+        if (r_ != HC_OK) return r_; \
+    } while (0)
+
+int check_status(hc_ctx *c)
+{
+    HC_CUDA(cudaMemcpyAsync(c->h_st, c->st, sizeof(hc_status), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    const hc_status &s = *c->h_st;
+    if (s.error == 0) return HC_OK;
+    char buf[256];
+    switch (s.error) {
+    case HC_ERR_CELLS:
+        snprintf(buf, sizeof buf, "makecell: need more than %d cells; increase fcells", s.info);
+        break;
+    case HC_ERR_COINCIDENT:
+        snprintf(buf, sizeof buf, "loadtree: body %d shares its integer coordinates with another body", s.info);
+        break;
+    case HC_ERR_STACK:
+        snprintf(buf, sizeof buf, "walk: traversal stack of %d entries exhausted", s.info);
+        break;
+    default:
+        snprintf(buf, sizeof buf, "device error %d (info %d)", s.error, s.info);
+    }
+    c->err = buf;
+    return s.error;
+}
+
+void free_all(hc_ctx *c)
+{
+    void *ptrs[] = {c->mass, c->px, c->py, c->pz, c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->phi, c->cnt_b,
+                    c->cnt_c, c->khi[0], c->khi[1], c->klo[0], c->klo[1], c->kval[0], c->kval[1], c->s_rank,
+                    c->leaf_of_sorted, c->mhi, c->mlo, c->midx, c->mpos, c->dlcp, c->ccount, c->pre_info, c->pre_a,
+                    c->pre_b, c->dkey[0], c->dkey[1], c->dval[0], c->dval[1], c->pre2bfs, c->parent, c->lastc,
+                    c->nodeA, c->nodeB, c->nodeQ, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->nq, c->flags,
+                    c->scan_tmp, c->hist, c->cand, c->ncand, c->diag_part, c->st, c->box, c->tx, c->ty, c->tz,
+                    c->tax, c->tay, c->taz, c->tphi, c->tkhi[0], c->tkhi[1], c->tklo[0], c->tklo[1],
+                    c->tkval[0], c->tkval[1]};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (c->h_st) cudaFreeHost(c->h_st);
+    if (c->h_box) cudaFreeHost(c->h_box);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+int alloc_all(hc_ctx *c)
+{
+    const int64_t n = c->n;
+    double **bd[] = {&c->mass, &c->px, &c->py, &c->pz, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->phi};
+    for (double **p : bd) HC_TRY(dalloc(c, p, n));
+    HC_TRY(dalloc(c, &c->cnt_b, n));
+    HC_TRY(dalloc(c, &c->cnt_c, n));
+    for (int i = 0; i < 2; i++) {
+        HC_TRY(dalloc(c, &c->khi[i], n));
+        HC_TRY(dalloc(c, &c->klo[i], n));
+        HC_TRY(dalloc(c, &c->kval[i], n));
+    }
+    HC_TRY(dalloc(c, &c->s_rank, n));
+    HC_TRY(dalloc(c, &c->leaf_of_sorted, n));
+    HC_TRY(dalloc(c, &c->mhi, n));
+    HC_TRY(dalloc(c, &c->mlo, n));
+    HC_TRY(dalloc(c, &c->midx, n));
+    HC_TRY(dalloc(c, &c->mpos, n));
+    HC_TRY(dalloc(c, &c->dlcp, n));
+    HC_TRY(dalloc(c, &c->ccount, n + 1));
+    const int64_t mn = c->maxnode;
+    HC_TRY(dalloc(c, &c->pre_info, mn));
+    HC_TRY(dalloc(c, &c->pre_a, mn));
+    HC_TRY(dalloc(c, &c->pre_b, mn));
+    for (int i = 0; i < 2; i++) {
+        HC_TRY(dalloc(c, &c->dkey[i], mn));
+        HC_TRY(dalloc(c, &c->dval[i], mn));
+    }
+    HC_TRY(dalloc(c, &c->pre2bfs, mn));
+    HC_TRY(dalloc(c, &c->parent, mn));
+    HC_TRY(dalloc(c, &c->lastc, mn));
+    HC_TRY(dalloc(c, &c->nodeA, mn));
+    HC_TRY(dalloc(c, &c->nodeB, mn));
+    HC_TRY(dalloc(c, &c->nodeQ, 2 * mn));
+    HC_TRY(dalloc(c, &c->nodeC, mn));
+    HC_TRY(dalloc(c, &c->nm, mn));
+    HC_TRY(dalloc(c, &c->ncx, mn));
+    HC_TRY(dalloc(c, &c->ncy, mn));
+    HC_TRY(dalloc(c, &c->ncz, mn));
+    HC_TRY(dalloc(c, &c->nq, 6 * mn));
+    HC_TRY(dalloc(c, &c->flags, 4 * n + 8));
+    HC_TRY(dalloc(c, &c->scan_tmp, 1024));
+    const int64_t big = std::max<int64_t>(n, mn);
+    HC_TRY(dalloc(c, &c->hist, 256 * ((big + 4095) / 4096) + 256));
+    HC_TRY(dalloc(c, &c->cand, n));
+    HC_TRY(dalloc(c, &c->ncand, 4));
+    HC_TRY(dalloc(c, &c->diag_part, 36 * 1024));
+    HC_TRY(dalloc(c, &c->st, 2));
+    HC_TRY(dalloc(c, &c->box, 1));
+    HC_CUDA(cudaMallocHost((void **)&c->h_st, sizeof(hc_status)));
+    HC_CUDA(cudaMallocHost((void **)&c->h_box, sizeof(hc_box)));
+    return HC_OK;
+}
+
+int ensure_test_capacity(hc_ctx *c, int64_t nt)
+{
+    if (nt <= c->tcap) return HC_OK;
+    void *ptrs[] = {c->tx, c->ty, c->tz, c->tax, c->tay, c->taz, c->tphi, c->tkhi[0], c->tkhi[1],
+                    c->tklo[0], c->tklo[1], c->tkval[0], c->tkval[1]};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    double **dd[] = {&c->tx, &c->ty, &c->tz, &c->tax, &c->tay, &c->taz, &c->tphi};
+    for (double **p : dd) HC_TRY(dalloc(c, p, nt));
+    for (int i = 0; i < 2; i++) {
+        HC_TRY(dalloc(c, &c->tkhi[i], nt));
+        HC_TRY(dalloc(c, &c->tklo[i], nt));
+        HC_TRY(dalloc(c, &c->tkval[i], nt));
+    }
+    // the radix sort histograms are sized for max(n, maxnode); grow if needed
+    if (nt > std::max<int64_t>(c->n, c->maxnode)) {
+        cudaFree(c->hist);
+        HC_TRY(dalloc(c, &c->hist, 256 * ((nt + 4095) / 4096) + 256));
+    }
+    c->tcap = nt;
+    return HC_OK;
+}
+
+void reset_status(hc_ctx *c) { cudaMemsetAsync(c->st, 0, sizeof(hc_status), c->stream); }
+
+// SoA <-> reference AoS layouts
+__global__ void k_unpack_phase(const double *phase, int64_t n, double *px, double *py, double *pz, double *vx,
+                               double *vy, double *vz)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double *q = phase + 6 * i;
+        px[i] = q[0];
+        py[i] = q[1];
+        pz[i] = q[2];
+        vx[i] = q[3];
+        vy[i] = q[4];
+        vz[i] = q[5];
+    }
+}
+
+__global__ void k_pack3(const double *x, const double *y, const double *z, int64_t n, double *out, int stride,
+                        int off)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        out[stride * i + off] = x[i];
+        out[stride * i + off + 1] = y[i];
+        out[stride * i + off + 2] = z[i];
+    }
+}
+
+__global__ void k_unpack3(const double *in, int64_t n, double *x, double *y, double *z)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = in[3 * i];
+        y[i] = in[3 * i + 1];
+        z[i] = in[3 * i + 2];
+    }
+}
+
+// staging buffer for host <-> device conversions (device side)
+struct Staging {
+    double *d = nullptr;
+    int64_t cap = 0;
+};
+
+int staging(hc_ctx *c, Staging &s, int64_t count)
+{
+    if (count <= s.cap) return HC_OK;
+    if (s.d) cudaFree(s.d);
+    s.d = nullptr;
+    HC_TRY(dalloc(c, &s.d, count));
+    s.cap = count;
+    return HC_OK;
+}
+
+}  // namespace
+
+struct hc_ctx_ext : hc_ctx {
+    Staging stage;
+    double *d_diag = nullptr;
+    int64_t *d_idx = nullptr;
+    int64_t idx_cap = 0;
+    double *d_out = nullptr;
+    int64_t out_cap = 0;
+};
+
+extern "C" {
+
+int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
+{
+    if (!out || nbody < 1 || !params) return HC_ERR_ARG;
+    if (nbody > (1LL << 28)) return HC_ERR_ARG;
+    hc_ctx_ext *c = new hc_ctx_ext();   // value-initialised: all pointers null
+    c->n = nbody;
+    c->prm = *params;
+    c->maxcell = (int64_t)(params->fcells * (double)nbody);   // load.c:50
+    if (c->maxcell < 1) c->maxcell = 1;
+    c->maxnode = nbody + c->maxcell;
+    *out = c;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        c->err = "cudaStreamCreate failed";
+        return HC_ERR_CUDA;
+    }
+    for (auto &e : c->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return HC_ERR_CUDA;
+    int r = alloc_all(c);
+    if (r != HC_OK) return r;
+    HC_CUDA(cudaMalloc((void **)&c->d_diag, 64 * sizeof(double)));
+    hc_box b;
+    std::memset(&b, 0, sizeof b);
+    b.rmin[0] = b.rmin[1] = b.rmin[2] = -2.0;   // code.c:119-120
+    b.rsize = 4.0;
+    b.first_massive = -1;
+    b.chain_lmax = b.chain_lmin = -1;
+    HC_CUDA(cudaMemcpy(c->box, &b, sizeof b, cudaMemcpyHostToDevice));
+    HC_CUDA(cudaMemset(c->st, 0, 2 * sizeof(hc_status)));
+    return HC_OK;
+}
+
+void hc_destroy(hc_ctx *ctx)
+{
+    if (!ctx) return;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->stage.d) cudaFree(c->stage.d);
+    if (c->d_diag) cudaFree(c->d_diag);
+    if (c->d_idx) cudaFree(c->d_idx);
+    if (c->d_out) cudaFree(c->d_out);
+    free_all(c);
+    delete c;
+}
+
+const char *hc_last_error(const hc_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int hc_set_params(hc_ctx *c, const hc_params *p)
+{
+    if (!c || !p) return HC_ERR_ARG;
+    if ((int64_t)(p->fcells * (double)c->n) != c->maxcell) {
+        c->err = "fcells is fixed when the context is created (load.c:49-53 allocates the cell pool once)";
+        return HC_ERR_ARG;
+    }
+    c->prm = *p;
+    return HC_OK;
+}
+
+int hc_upload(hc_ctx *ctx, const double *mass, const double *phase)
+{
+    if (!ctx || !mass || !phase) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    const int64_t n = c->n;
+    HC_TRY(staging(c, c->stage, 6 * n));
+    HC_CUDA(cudaMemcpyAsync(c->mass, mass, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    HC_CUDA(cudaMemcpyAsync(c->stage.d, phase, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, c->stream));
+    k_unpack_phase<<<hc_grid(n, 256), 256, 0, c->stream>>>(c->stage.d, n, c->px, c->py, c->pz, c->vx, c->vy, c->vz);
+    HC_CUDA(cudaMemsetAsync(c->ax, 0, sizeof(double) * n, c->stream));
+    HC_CUDA(cudaMemsetAsync(c->ay, 0, sizeof(double) * n, c->stream));
+    HC_CUDA(cudaMemsetAsync(c->az, 0, sizeof(double) * n, c->stream));
+    HC_CUDA(cudaMemsetAsync(c->phi, 0, sizeof(double) * n, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    c->have_tree = c->have_forces = false;
+    return HC_OK;
+}
+
+int hc_set_box(hc_ctx *c, const double rmin[3], double rsize)
+{
+    if (!c || !rmin || !(rsize > 0)) return HC_ERR_ARG;
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaMemcpy(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 3; k++) c->h_box->rmin[k] = rmin[k];
+    c->h_box->rsize = rsize;
+    HC_CUDA(cudaMemcpy(c->box, c->h_box, sizeof(hc_box), cudaMemcpyHostToDevice));
+    c->have_tree = false;
+    return HC_OK;
+}
+
+int hc_get_box(hc_ctx *c, double rmin[3], double *rsize)
+{
+    if (!c || !rmin || !rsize) return HC_ERR_ARG;
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaMemcpy(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 3; k++) rmin[k] = c->h_box->rmin[k];
+    *rsize = c->h_box->rsize;
+    return HC_OK;
+}
+
+int hc_build_tree(hc_ctx *c)
+{
+    if (!c) return HC_ERR_ARG;
+    c->launches = 0;
+    reset_status(c);
+    HC_CUDA(cudaEventRecord(c->ev[0], c->stream));
+    int r = hc_tree_build(c);
+    if (r != HC_OK) {
+        check_status(c);
+        return r;
+    }
+    HC_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    r = check_status(c);
+    if (r != HC_OK) return r;
+    cudaEventElapsedTime(&c->build_ms, c->ev[0], c->ev[1]);
+    c->have_tree = true;
+    c->have_forces = false;
+    return HC_OK;
+}
+
+int hc_tree_summary(hc_ctx *c, hc_tree_info *info)
+{
+    if (!c || !info) return HC_ERR_ARG;
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaMemcpy(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost));
+    info->nbody_massive = c->h_box->nmassive;
+    info->ncell = c->h_box->ncell;
+    info->max_level = c->h_box->max_depth;
+    for (int k = 0; k < 3; k++) info->rmin[k] = c->h_box->rmin[k];
+    info->rsize = c->h_box->rsize;
+    return HC_OK;
+}
+
+int hc_dump_tree(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count, double *mass, double *cm,
+                 double *quad, int32_t *body_parent_level)
+{
+    if (!c) return HC_ERR_ARG;
+    if (!c->have_tree) {
+        c->err = "hc_dump_tree: no tree (call hc_build_tree first)";
+        return HC_ERR_STATE;
+    }
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    int r = hc_tree_dump_impl(c, level, corner, count, mass, cm, quad, body_parent_level);
+    return r < 0 ? r : HC_OK;
+}
+
+static int forces_self(hc_ctx *c, double kick_dthf, int64_t nstep)
+{
+    if (!c->have_tree) {
+        c->err = "forces requested before hc_build_tree";
+        return HC_ERR_STATE;
+    }
+    reset_status(c);
+    HC_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    HC_TRY(hc_walk_launch(c, true, c->n, c->sidx, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
+                          nstep));
+    HC_CUDA(cudaEventRecord(c->ev[3], c->stream));
+    HC_TRY(check_status(c));
+    cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]);
+    c->have_forces = true;
+    return HC_OK;
+}
+
+int hc_forces(hc_ctx *c)
+{
+    if (!c) return HC_ERR_ARG;
+    return forces_self(c, 0.0, 0);
+}
+
+int hc_forces_at(hc_ctx *ctx, const double *test_pos, int64_t ntest, double *acc, double *phi)
+{
+    if (!ctx || ntest < 0 || (ntest > 0 && (!test_pos || !acc || !phi))) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    if (!c->have_tree) {
+        c->err = "hc_forces_at before hc_build_tree";
+        return HC_ERR_STATE;
+    }
+    if (ntest == 0) return HC_OK;
+    HC_TRY(ensure_test_capacity(c, ntest));
+    HC_TRY(staging(c, c->stage, 3 * ntest));
+    reset_status(c);
+    HC_CUDA(cudaMemcpyAsync(c->stage.d, test_pos, sizeof(double) * 3 * ntest, cudaMemcpyHostToDevice, c->stream));
+    k_unpack3<<<hc_grid(ntest, 256), 256, 0, c->stream>>>(c->stage.d, ntest, c->tx, c->ty, c->tz);
+    hc_keys_for_points(c, c->tx, c->ty, c->tz, ntest, c->tkhi[0], c->tklo[0], c->tkval[0]);
+    int sel = hc_radix_sort_keys(c, c->tkhi, c->tklo, c->tkval, ntest, 0, 64, false);
+    HC_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    HC_TRY(hc_walk_launch(c, false, ntest, c->tkval[sel], c->tx, c->ty, c->tz, c->tax, c->tay, c->taz, c->tphi,
+                          0.0, 0));
+    HC_CUDA(cudaEventRecord(c->ev[3], c->stream));
+    k_pack3<<<hc_grid(ntest, 256), 256, 0, c->stream>>>(c->tax, c->tay, c->taz, ntest, c->stage.d, 3, 0);
+    HC_CUDA(cudaMemcpyAsync(acc, c->stage.d, sizeof(double) * 3 * ntest, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaMemcpyAsync(phi, c->tphi, sizeof(double) * ntest, cudaMemcpyDeviceToHost, c->stream));
+    HC_TRY(check_status(c));
+    cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]);
+    return HC_OK;
+}
+
+int hc_download(hc_ctx *ctx, double *phase, double *acc, double *phi)
+{
+    if (!ctx) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    const int64_t n = c->n;
+    HC_TRY(staging(c, c->stage, 6 * n));
+    if (phase) {
+        k_pack3<<<hc_grid(n, 256), 256, 0, c->stream>>>(c->px, c->py, c->pz, n, c->stage.d, 6, 0);
+        k_pack3<<<hc_grid(n, 256), 256, 0, c->stream>>>(c->vx, c->vy, c->vz, n, c->stage.d, 6, 3);
+        HC_CUDA(cudaMemcpyAsync(phase, c->stage.d, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, c->stream));
+        HC_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    if (acc) {
+        k_pack3<<<hc_grid(n, 256), 256, 0, c->stream>>>(c->ax, c->ay, c->az, n, c->stage.d, 3, 0);
+        HC_CUDA(cudaMemcpyAsync(acc, c->stage.d, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+        HC_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    if (phi) HC_CUDA(cudaMemcpyAsync(phi, c->phi, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int hc_body_counts(hc_ctx *c, int32_t *n2b, int32_t *nbc)
+{
+    if (!c) return HC_ERR_ARG;
+    if (!c->prm.count_per_body || !c->have_forces) {
+        c->err = "hc_body_counts: needs count_per_body and a completed hc_forces";
+        return HC_ERR_STATE;
+    }
+    if (n2b) HC_CUDA(cudaMemcpyAsync(n2b, c->cnt_b, sizeof(int32_t) * c->n, cudaMemcpyDeviceToHost, c->stream));
+    if (nbc) HC_CUDA(cudaMemcpyAsync(nbc, c->cnt_c, sizeof(int32_t) * c->n, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    return HC_OK;
+}
+
+static int fill_diag(hc_ctx_ext *c, hc_diag *d)
+{
+    double h[36];
+    hc_diag_launch(c, c->d_diag);
+    HC_CUDA(cudaMemcpyAsync(h, c->d_diag, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    std::memset(d, 0, sizeof *d);
+    d->etot[1] = h[0];
+    d->etot[2] = h[1];
+    d->etot[0] = d->etot[1] + d->etot[2];
+    for (int k = 0; k < 9; k++) {
+        d->keten[k] = h[2 + k];
+        d->peten[k] = h[11 + k];
+    }
+    for (int j = 0; j < 3; j++)
+        for (int k = 0; k < 3; k++) d->amten[3 * j + k] = h[20 + 3 * j + k] - h[20 + 3 * k + j];
+    d->mtot = h[35];
+    for (int k = 0; k < 3; k++) {
+        d->cmphase[k] = h[29 + k] / d->mtot;
+        d->cmphase[3 + k] = h[32 + k] / d->mtot;
+    }
+    d->n2b = (int64_t)c->h_st->n2b;
+    d->nbc = (int64_t)c->h_st->nbc;
+    d->nfcalc = c->n;
+    return HC_OK;
+}
+
+int hc_diagnostics(hc_ctx *ctx, hc_diag *diag)
+{
+    if (!ctx || !diag) return HC_ERR_ARG;
+    return fill_diag(static_cast<hc_ctx_ext *>(ctx), diag);
+}
+
+int hc_step(hc_ctx *ctx, double dt, int64_t nstep, hc_diag *diag, double *snap_phase, double *snap_acc,
+            double *snap_phi)
+{
+    if (!ctx || !(dt > 0)) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    HC_TRY(hc_build_tree(c));
+    HC_TRY(forces_self(c, 0.5 * dt, nstep));
+    if (diag) HC_TRY(fill_diag(c, diag));
+    if (snap_phase || snap_acc || snap_phi) HC_TRY(hc_download(c, snap_phase, snap_acc, snap_phi));
+    hc_kick_drift(c, dt);
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    c->have_tree = false;
+    return HC_OK;
+}
+
+int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t ns, double *acc, double *phi)
+{
+    if (!ctx || ns < 0 || (ns > 0 && (!index || !acc || !phi))) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    for (int64_t i = 0; i < ns; i++)
+        if (index[i] < 0 || index[i] >= c->n) {
+            c->err = "hc_direct_sample: index out of range";
+            return HC_ERR_ARG;
+        }
+    if (ns == 0) return HC_OK;
+    if (ns > c->idx_cap) {
+        if (c->d_idx) cudaFree(c->d_idx);
+        if (c->d_out) cudaFree(c->d_out);
+        c->d_idx = nullptr;
+        c->d_out = nullptr;
+        HC_TRY(dalloc(c, &c->d_idx, ns));
+        HC_TRY(dalloc(c, &c->d_out, 4 * ns));
+        c->idx_cap = ns;
+    }
+    HC_CUDA(cudaMemcpyAsync(c->d_idx, index, sizeof(int64_t) * ns, cudaMemcpyHostToDevice, c->stream));
+    hc_direct_launch(c, c->d_idx, ns, c->d_out, c->d_out + 3 * ns);
+    HC_CUDA(cudaMemcpyAsync(acc, c->d_out, sizeof(double) * 3 * ns, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaMemcpyAsync(phi, c->d_out + 3 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int hc_timer_start(hc_ctx *c)
+{
+    if (!c) return HC_ERR_ARG;
+    HC_CUDA(cudaEventRecord(c->ev[4], c->stream));
+    return HC_OK;
+}
+
+int hc_timer_stop(hc_ctx *c, double *ms)
+{
+    if (!c || !ms) return HC_ERR_ARG;
+    HC_CUDA(cudaEventRecord(c->ev[5], c->stream));
+    HC_CUDA(cudaEventSynchronize(c->ev[5]));
+    float f = 0.f;
+    HC_CUDA(cudaEventElapsedTime(&f, c->ev[4], c->ev[5]));
+    *ms = f;
+    return HC_OK;
+}
+
+int hc_fp32_peak(hc_ctx *c, double *tflops)
+{
+    if (!c || !tflops) return HC_ERR_ARG;
+    return hc_fma_peak_impl(c, tflops);
+}
+
+int hc_last_timing(hc_ctx *c, double *build_ms, double *walk_ms, int64_t *launches)
+{
+    if (!c) return HC_ERR_ARG;
+    if (build_ms) *build_ms = c->build_ms;
+    if (walk_ms) *walk_ms = c->walk_ms;
+    if (launches) *launches = c->launches;
+    return HC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+// hc_internal.cuh -- shared definitions of the GB300 hackcode1 library.
+//
+// Data layout in HBM (one context = one system of nbody bodies):
+//   bodies, original order, FP64 SoA: mass, pos[3], vel[3], acc[3], phi
+//   keys, sorted order: 63-bit high key (top 21 bits per axis, Morton
+//     interleaved, x most significant) + 27-bit low key + original index
+//   tree nodes (bodies and cells) in breadth-first order, children of a
+//     cell contiguous and in subindex order 0..7 (load.c:162-177):
+//       nodeA float4 (cm_hi.xyz, mass)   nodeB float4 (cm_lo.xyz, size^2)
+//       nodeC int2   (first child | -1-body slot, nchild | depth<<8)
+//       nodeQ 2 x float4 (Qxx Qxy Qxz Qyy | Qyz Qzz 0 0)
+//       FP64 mass / cm / quad per node for the upward pass and for exact
+//       re-evaluation of borderline opening decisions.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "../../include/hackcode_gpu.h"
+
+#define HC_IMAX (1 << 30)     // defs.h:124-128
+#define HC_MAXLEVEL 31        // levels 0..30
+
+// Device status word (written by kernels, read by the host after a sync).
+struct hc_status {
+    int error;                // 0 or HC_ERR_*
+    int info;
+    unsigned long long n2b;   // interaction totals of the last walk
+    unsigned long long nbc;
+    int max_stack;            // deepest walk stack seen
+    int nborder;              // borderline opening decisions re-done in FP64
+};
+
+// Root box state, kept on the device so the whole step can run without a
+// host round trip (expandbox replay happens on the GPU).
+struct hc_box {
+    double rmin[3];
+    double rsize;
+    int chain_body;           // original index of the first massive body or -1
+    int chain_lmax;           // deepest one-body expansion cell level (or -1)
+    int chain_lmin;
+    int nmassive;             // massive bodies
+    int first_massive;        // original index of the first massive body
+    int ncell;                // cells of the last build
+    int max_depth;            // deepest node depth of the last build
+    int nnode;                // nmassive + ncell
+    int level_start[HC_MAXLEVEL + 2];  // BFS offset of each depth
+    double dsq[HC_MAXLEVEL + 1];       // rsize^2 / 4^level (grav.c:86,105)
+};
+
+struct hc_ctx {
+    int64_t n;                // bodies
+    int64_t maxcell;          // (int)(fcells * n), load.c:50
+    hc_params prm;
+    cudaStream_t stream;
+    cudaEvent_t ev[6];        // 0-1 build, 2-3 walk, 4-5 user timer
+    std::string err;
+    bool have_tree, have_forces;
+    int64_t launches;
+    float build_ms, walk_ms;
+
+    // bodies (original order)
+    double *mass, *px, *py, *pz, *vx, *vy, *vz, *ax, *ay, *az, *phi;
+    int32_t *cnt_b, *cnt_c;   // per-body counts (optional)
+
+    // keys and sort (n entries, double-buffered)
+    unsigned long long *khi[2];
+    uint32_t *klo[2];
+    uint32_t *kval[2];
+    int sort_sel;             // which buffer holds the sorted result
+    uint32_t *sidx;           // sorted position -> original index (all bodies)
+    int32_t *s_rank;          // sorted position -> massive rank or -1
+    int32_t *leaf_of_sorted;  // sorted position -> BFS node of its leaf or -1
+
+    // massive bodies in key order
+    unsigned long long *mhi;
+    uint32_t *mlo;
+    uint32_t *midx;           // massive rank -> original index
+    uint32_t *mpos;           // massive rank -> sorted position
+    int32_t *dlcp;            // lcp in octal digits of adjacent massive keys
+    int32_t *ccount;          // cells starting at each massive rank (scan -> offsets)
+
+    // nodes
+    int64_t maxnode;
+    int32_t *pre_info;        // pre-order: level (cell) or -1 (body); bit 31 unused
+    int32_t *pre_a;           // pre-order: massive rank of first body
+    int32_t *pre_b;           // pre-order: massive rank of last body
+    unsigned long long *dkey[2]; // depth sort keys
+    uint32_t *dval[2];
+    uint32_t *bfs2pre, *pre2bfs;
+    int32_t *parent, *lastc;
+    float4 *nodeA, *nodeB, *nodeQ;
+    int2 *nodeC;
+    double *nm, *ncx, *ncy, *ncz, *nq;    // nq: 6 per node
+
+    // scratch
+    int32_t *flags;           // n
+    int32_t *scan_tmp;        // block partials
+    uint32_t *hist;           // radix histograms
+    int32_t *cand;            // expandbox candidates (original indices)
+    int32_t *ncand;
+    double *diag_part;        // per-block diagnostics partials
+    hc_status *st;            // device status
+    hc_box *box;              // device box
+    hc_status *h_st;          // pinned host mirrors
+    hc_box *h_box;
+
+    // test points for hc_forces_at
+    int64_t tcap;
+    double *tx, *ty, *tz, *tax, *tay, *taz, *tphi;
+    unsigned long long *tkhi[2];
+    uint32_t *tklo[2], *tkval[2];
+};
+
+// ---- host-side launchers implemented in the .cu files ----
+// scan / sort (hc_sort.cu)
+void hc_scan_exclusive_i32(hc_ctx *c, const int32_t *in, int32_t *out, int64_t n, int32_t *total_dev);
+int hc_radix_sort_keys(hc_ctx *c, unsigned long long *khi[2], uint32_t *klo[2], uint32_t *kval[2],
+                       int64_t n, int begin_bit, int end_bit, bool tie_fix);
+// tree (hc_tree.cu)
+int hc_tree_build(hc_ctx *c);
+int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count, double *mass,
+                      double *cm, double *quad, int32_t *bparent);
+void hc_keys_for_points(hc_ctx *c, const double *x, const double *y, const double *z, int64_t n,
+                        unsigned long long *khi, uint32_t *klo, uint32_t *kval);
+// walk (hc_walk.cu)
+int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorted,
+                   const double *tx, const double *ty, const double *tz, double *oax, double *oay,
+                   double *oaz, double *ophi, double kick_dthf, int64_t nstep);
+// step (hc_step.cu)
+void hc_kick_drift(hc_ctx *c, double dt);
+void hc_diag_launch(hc_ctx *c, double *out36);
+void hc_direct_launch(hc_ctx *c, const int64_t *idx_dev, int64_t ns, double *oacc, double *ophi);
+int hc_fma_peak_impl(hc_ctx *c, double *tflops);
+
+#define HC_CUDA(call)                                                               \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            c->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+            return HC_ERR_CUDA;                                                     \
+        }                                                                           \
+    } while (0)
+
+static inline int hc_grid(int64_t n, int block, int cap = 152 * 16)
+{
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}

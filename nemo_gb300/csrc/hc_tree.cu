@@ -1,0 +1,696 @@
+// hc_tree.cu -- octree construction and moments on the GPU.
+//
+// Reference: maketree/expandbox/loadtree/intcoord/subindex/hackcofm,
+// src/nbody/evolve/hackcode/hackcode1/load.c:32-248.
+//
+// The reference inserts massive bodies one at a time.  Its final tree is a
+// pure function of the root box and the multiset of integer coordinates: a
+// cell exists for every octree node (integer prefix) holding two or more
+// massive bodies, bodies are leaves, there is no leaf bucket and no path
+// compression.  The one exception is expandbox (load.c:68-95): when the second
+// massive body forces the box to double K >= 2 times, the K-1 intermediate
+// root cells hold only the first body.  The build here reproduces that set:
+//
+//   1. expandbox replay on the device (one block, FP64, body order),
+//   2. 90-bit keys: floor(2^30 (x - rmin) / rsize) per axis, Morton order,
+//   3. radix sort, compaction of the massive bodies,
+//   4. d[a] = common octal digits of adjacent keys; cells starting at sorted
+//      body a have levels (d[a-1], d[a]], which lays cells and bodies out in
+//      DFS pre-order directly,
+//   5. stable sort of the pre-order by depth -> breadth-first layout with the
+//      children of each cell contiguous and in subindex order 0..7,
+//   6. level-synchronous upward pass, FP64, children summed in the same order
+//      as hackcofm so mass, centre of mass and quadrupole are bit-identical.
+#include <memory>
+#include "hc_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// intcoord (load.c:135-156): xsc = (x - rmin)/rsize; inside iff 0 <= xsc < 1.
+__device__ __forceinline__ bool intcoord1(double x, double rmin, double rsize, int *xi)
+{
+    double xsc = ddiv(dsub(x, rmin), rsize);
+    if (0.0 <= xsc && xsc < 1.0) {
+        *xi = (int)floor(dmul((double)HC_IMAX, xsc));
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool inbox(double x, double y, double z, const double *rmin, double rsize)
+{
+    int t;
+    bool a = intcoord1(x, rmin[0], rsize, &t);
+    bool b = intcoord1(y, rmin[1], rsize, &t);
+    bool c = intcoord1(z, rmin[2], rsize, &t);
+    return a && b && c;
+}
+
+// ---------------- expandbox replay ----------------
+
+__global__ void k_box_flags(const double *mass, const double *px, const double *py, const double *pz,
+                            int64_t n, const hc_box *box, int32_t *outside, int32_t *massive)
+{
+    double rmin[3] = {box->rmin[0], box->rmin[1], box->rmin[2]};
+    double rsize = box->rsize;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        bool m = mass[i] != 0.0;
+        massive[i] = m;
+        outside[i] = m && !inbox(px[i], py[i], pz[i], rmin, rsize);
+    }
+}
+
+__global__ void k_box_compact(const int32_t *outside, const int32_t *opos, int64_t n, int32_t *cand)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (outside[i]) cand[opos[i]] = (int32_t)i;
+}
+
+// One block replays expandbox over the bodies that were outside the box at
+// the start, in body order.  The box only grows, so a body inside stays
+// inside; each round finds the first remaining body outside, expands for
+// it, and continues after it.
+__global__ void k_box_replay(const double *px, const double *py, const double *pz, const int32_t *cand,
+                             const int32_t *ncand_p, const int32_t *mrank, hc_box *box)
+{
+    __shared__ int first;
+    __shared__ double rmin[3], rsize;
+    __shared__ int doublings, chain_before, chain_k;
+    const int ncand = *ncand_p;
+    if (threadIdx.x == 0) {
+        rmin[0] = box->rmin[0];
+        rmin[1] = box->rmin[1];
+        rmin[2] = box->rmin[2];
+        rsize = box->rsize;
+        doublings = 0;
+        chain_before = -1;
+        chain_k = 0;
+    }
+    __syncthreads();
+    int pos = 0;
+    while (pos < ncand) {
+        if (threadIdx.x == 0) first = INT_MAX;
+        __syncthreads();
+        for (int base = pos; base < ncand; base += blockDim.x) {
+            int i = base + threadIdx.x;
+            if (i < ncand) {
+                int b = cand[i];
+                if (!inbox(px[b], py[b], pz[b], rmin, rsize)) atomicMin(&first, i);
+            }
+            __syncthreads();
+            if (first != INT_MAX) break;
+            __syncthreads();
+        }
+        int f = first;
+        __syncthreads();
+        if (f == INT_MAX) break;
+        if (threadIdx.x == 0) {
+            int b = cand[f];
+            double x[3] = {px[b], py[b], pz[b]};
+            int k = 0;
+            while (!inbox(x[0], x[1], x[2], rmin, rsize)) {     // load.c:74-93
+                if (k >= 1100) {          // non-finite position: the box can never hold it
+                    doublings = -1000000;
+                    break;
+                }
+                double rmid[3];
+                for (int d = 0; d < 3; d++) rmid[d] = dadd(rmin[d], dmul(0.5, rsize));
+                for (int d = 0; d < 3; d++)
+                    if (x[d] < rmid[d]) rmin[d] = dsub(rmin[d], rsize);
+                rsize = dmul(2.0, rsize);
+                k++;
+            }
+            if (mrank[b] == 1 && k >= 2) {   // grafted over a lone first body
+                chain_before = doublings;
+                chain_k = k;
+            }
+            doublings += k;
+        }
+        __syncthreads();
+        pos = f + 1;
+    }
+    if (threadIdx.x == 0 && doublings < 0) box->chain_lmin = -2;   // flagged below
+    if (threadIdx.x == 0) {
+        box->rmin[0] = rmin[0];
+        box->rmin[1] = rmin[1];
+        box->rmin[2] = rmin[2];
+        box->rsize = rsize;
+        if (chain_before >= 0) {
+            int e = doublings - chain_before;       // levels between that box and the final root
+            box->chain_lmax = e - 1;
+            box->chain_lmin = e - chain_k + 1;
+        } else {
+            box->chain_lmax = -1;
+            box->chain_lmin = -1;
+        }
+        double d = dmul(rsize, rsize);
+        for (int l = 0; l <= HC_MAXLEVEL; l++) {
+            box->dsq[l] = d;
+            d = ddiv(d, 4.0);
+        }
+    }
+}
+
+// first massive body (original order) for the expansion-chain cells
+__global__ void k_first_massive(const int32_t *massive, const int32_t *mrank, int64_t n, hc_box *box)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (massive[i] && mrank[i] == 0) box->first_massive = (int)i;
+}
+
+// ---------------- keys ----------------
+
+__device__ __forceinline__ unsigned long long spread21(unsigned v)
+{
+    unsigned long long x = v & 0x1fffffull;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t spread9(unsigned v)
+{
+    uint32_t x = v & 0x1ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__device__ __forceinline__ int intcoord_clamped(double x, double rmin, double rsize)
+{
+    int xi;
+    if (intcoord1(x, rmin, rsize, &xi)) return xi;
+    double xsc = ddiv(dsub(x, rmin), rsize);
+    return xsc < 0.0 ? 0 : HC_IMAX - 1;   // massless bodies / test points outside the box
+}
+
+__global__ void k_keys(const double *x, const double *y, const double *z, int64_t n, const hc_box *box,
+                       unsigned long long *khi, uint32_t *klo, uint32_t *kval)
+{
+    double r0 = box->rmin[0], r1 = box->rmin[1], r2 = box->rmin[2], rs = box->rsize;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        unsigned ix = intcoord_clamped(x[i], r0, rs), iy = intcoord_clamped(y[i], r1, rs),
+                 iz = intcoord_clamped(z[i], r2, rs);
+        khi[i] = (spread21(ix >> 9) << 2) | (spread21(iy >> 9) << 1) | spread21(iz >> 9);
+        klo[i] = (spread9(ix) << 2) | (spread9(iy) << 1) | spread9(iz);
+        kval[i] = (uint32_t)i;
+    }
+}
+
+// ---------------- massive compaction and cell enumeration ----------------
+
+__global__ void k_sorted_massive(const uint32_t *sidx, const double *mass, int64_t n, int32_t *flag)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x)
+        flag[s] = mass[sidx[s]] != 0.0;
+}
+
+__global__ void k_mcompact(const int32_t *flag, const int32_t *rank, int64_t n, const unsigned long long *khi,
+                           const uint32_t *klo, const uint32_t *sidx, unsigned long long *mhi, uint32_t *mlo,
+                           uint32_t *midx, uint32_t *mpos, int32_t *s_rank, int32_t *leaf_of_sorted)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        leaf_of_sorted[s] = -1;
+        if (flag[s]) {
+            int r = rank[s];
+            mhi[r] = khi[s];
+            mlo[r] = klo[s];
+            midx[r] = sidx[s];
+            mpos[r] = (uint32_t)s;
+            s_rank[s] = r;
+        } else
+            s_rank[s] = -1;
+    }
+}
+
+// common leading octal digits of two 90-bit keys (30 = identical)
+__device__ __forceinline__ int lcp_digits(unsigned long long ha, uint32_t la, unsigned long long hb, uint32_t lb)
+{
+    unsigned long long x = ha ^ hb;
+    if (x) return (__clzll(x) - 1) / 3;
+    uint32_t y = la ^ lb;
+    if (y) return 21 + (__clz(y) - 5) / 3;
+    return 30;
+}
+
+__device__ __forceinline__ int dprime(const int32_t *d, const uint32_t *midx, int a, const hc_box *box)
+{
+    int v = d[a];
+    if ((int)midx[a] == box->first_massive && box->chain_lmax > v) v = box->chain_lmax;
+    return v;
+}
+
+__global__ void k_lcp(const unsigned long long *mhi, const uint32_t *mlo, const uint32_t *midx, hc_box *box,
+                      int32_t *d, hc_status *st)
+{
+    const int M = box->nmassive;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < M; a += gridDim.x * blockDim.x) {
+        int v = -1;
+        if (a + 1 < M) {
+            v = lcp_digits(mhi[a], mlo[a], mhi[a + 1], mlo[a + 1]);
+            if (v >= 30) {                     // assert(l != 0), load.c:113
+                atomicCAS(&st->error, 0, HC_ERR_COINCIDENT);
+                st->info = (int)midx[a];
+                v = 29;
+            }
+        }
+        d[a] = v;
+    }
+}
+
+__global__ void k_ccount(const int32_t *d, const uint32_t *midx, const hc_box *box, int32_t *ccount)
+{
+    const int M = box->nmassive;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < M; a += gridDim.x * blockDim.x) {
+        int dp = a > 0 ? d[a - 1] : -1;
+        int dm = dprime(d, midx, a, box);
+        ccount[a] = dm > dp ? dm - dp : 0;
+    }
+}
+
+__global__ void k_post_count(int32_t *cstart, hc_box *box, int64_t maxcell, hc_status *st)
+{
+    const int M = box->nmassive;
+    int ncell = cstart[M];
+    box->ncell = ncell;
+    box->nnode = M + ncell;
+    if (ncell > maxcell) {                      // makecell, load.c:237-239
+        atomicCAS(&st->error, 0, HC_ERR_CELLS);
+        st->info = (int)maxcell;
+    }
+}
+
+// Pre-order layout: for each sorted massive body a, the cells that start
+// at a (levels dprev+1 .. d'[a], outermost first), then body a itself.
+__global__ void k_emit_preorder(const int32_t *d, const uint32_t *midx, const int32_t *cstart, const hc_box *box,
+                                int64_t maxnode, int32_t *pre_depth, int32_t *pre_a,
+                                unsigned long long *dkey, uint32_t *dval)
+{
+    const int M = box->nmassive;
+    if (box->nnode > maxnode) return;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < M; a += gridDim.x * blockDim.x) {
+        int dp = a > 0 ? d[a - 1] : -1;
+        int dm = dprime(d, midx, a, box);
+        int base = a + cstart[a];
+        int p = base;
+        for (int L = dp + 1; L <= dm; L++, p++) {
+            pre_depth[p] = L;
+            pre_a[p] = a;
+            dkey[p] = (unsigned long long)L;
+            dval[p] = (uint32_t)p;
+        }
+        int depth = (dp > dm ? dp : dm) + 1;    // parent is the deepest cell holding a
+        p = a + cstart[a + 1];
+        pre_depth[p] = depth;
+        pre_a[p] = -1 - a;
+        dkey[p] = (unsigned long long)depth;
+        dval[p] = (uint32_t)p;
+    }
+}
+
+// Last body of each cell: the largest j with lcp(key a, key j) >= level.
+__global__ void k_cell_end(const unsigned long long *mhi, const uint32_t *mlo, const int32_t *d,
+                           const int32_t *pre_depth, const int32_t *pre_a, const hc_box *box, int64_t maxnode,
+                           int32_t *pre_b)
+{
+    const int nn = box->nnode, M = box->nmassive;
+    if (nn > maxnode) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nn; p += gridDim.x * blockDim.x) {
+        int a = pre_a[p];
+        if (a < 0) continue;
+        int L = pre_depth[p];
+        if (d[a] < L) {             // one-body expansion cell
+            pre_b[p] = a;
+            continue;
+        }
+        unsigned long long ha = mhi[a];
+        uint32_t la = mlo[a];
+        int step = 1;
+        while (a + step < M && lcp_digits(ha, la, mhi[a + step], mlo[a + step]) >= L) step <<= 1;
+        int lo = a + (step >> 1), hi = min(a + step, M - 1);   // lcp(lo) >= L holds
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (lcp_digits(ha, la, mhi[mid], mlo[mid]) >= L) lo = mid;
+            else hi = mid - 1;
+        }
+        pre_b[p] = lo;
+    }
+}
+
+__global__ void k_levels(const uint32_t *offs, int nblk, hc_box *box)
+{
+    // offs is the scanned depth histogram (digit-major); digit D starts at offs[D*nblk]
+    int D = threadIdx.x;
+    if (D <= HC_MAXLEVEL + 1) {
+        int v = D <= HC_MAXLEVEL ? (int)offs[(int64_t)D * nblk] : box->nnode;
+        box->level_start[D] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int md = 0;
+        for (int l = 0; l <= HC_MAXLEVEL; l++)
+            if (box->level_start[l + 1] > box->level_start[l]) md = l;
+        box->max_depth = md;
+    }
+}
+
+__global__ void k_pre2bfs(const uint32_t *bfs2pre, const hc_box *box, uint32_t *pre2bfs)
+{
+    const int nn = box->nnode;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x)
+        pre2bfs[bfs2pre[k]] = (uint32_t)k;
+}
+
+// parent = the node one level up with the largest pre-order index below ours
+__global__ void k_parent(const uint32_t *bfs2pre, const int32_t *pre_depth, const hc_box *box, int32_t *parent)
+{
+    const int nn = box->nnode;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+        uint32_t p = bfs2pre[k];
+        int D = pre_depth[p];
+        if (D == 0) {
+            parent[k] = -1;
+            continue;
+        }
+        int lo = box->level_start[D - 1], hi = box->level_start[D] - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (bfs2pre[mid] < p) lo = mid;
+            else hi = mid - 1;
+        }
+        parent[k] = lo;
+    }
+}
+
+__global__ void k_children(const int32_t *parent, const uint32_t *bfs2pre, const int32_t *pre_depth,
+                           const hc_box *box, int2 *nodeC, int32_t *lastc)
+{
+    const int nn = box->nnode;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+        int p = parent[k];
+        if (p < 0) continue;
+        int D = pre_depth[bfs2pre[k]];
+        int ls = box->level_start[D], le = box->level_start[D + 1];
+        if (k == ls || parent[k - 1] != p) nodeC[p].x = k;
+        if (k + 1 == le || parent[k + 1] != p) lastc[p] = k;
+    }
+}
+
+__device__ __forceinline__ void split_hilo(double v, float *hi, float *lo)
+{
+    float h = __double2float_rn(v);
+    *hi = h;
+    *lo = __double2float_rn(dsub(v, (double)h));
+}
+
+// Node fields that do not need the upward pass: body leaves (mass and
+// position from the body arrays) and the child range of every cell.
+__global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, const int32_t *pre_a,
+                            const uint32_t *midx, const uint32_t *mpos, const double *mass, const double *px,
+                            const double *py, const double *pz, const hc_box *box, int2 *nodeC,
+                            const int32_t *lastc, float4 *nodeA, float4 *nodeB, float4 *nodeQ, double *nm,
+                            double *ncx, double *ncy, double *ncz, double *nq, int32_t *leaf_of_sorted,
+                            hc_status *st)
+{
+    const int nn = box->nnode;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+        uint32_t p = bfs2pre[k];
+        int D = pre_depth[p], a = pre_a[p];
+        if (a < 0) {
+            a = -1 - a;
+            uint32_t o = midx[a], s = mpos[a];
+            double m = mass[o], x = px[o], y = py[o], z = pz[o];
+            nm[k] = m;
+            ncx[k] = x;
+            ncy[k] = y;
+            ncz[k] = z;
+            for (int q = 0; q < 6; q++) nq[(int64_t)6 * k + q] = 0.0;
+            float4 A, B;
+            split_hilo(x, &A.x, &B.x);
+            split_hilo(y, &A.y, &B.y);
+            split_hilo(z, &A.z, &B.z);
+            A.w = __double2float_rn(m);
+            B.w = -1.0f;
+            nodeA[k] = A;
+            nodeB[k] = B;
+            nodeQ[2 * (int64_t)k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            nodeQ[2 * (int64_t)k + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            nodeC[k] = make_int2(-1 - (int)s, D << 8);
+            leaf_of_sorted[s] = k;
+        } else {
+            int fc = nodeC[k].x, nc = lastc[k] - fc + 1;
+            if (fc <= k || nc < 1 || nc > 8 || fc + nc > nn) {   // children follow their parent
+                atomicCAS(&st->error, 0, HC_ERR_STATE);
+                st->info = k;
+                fc = k + 1;
+                nc = 0;
+            }
+            nodeC[k] = make_int2(fc, nc | (D << 8));
+        }
+    }
+}
+
+// hackcofm (load.c:183-226) for the cells of one level, children in order.
+__global__ void k_cofm_level(int D, int usequad, const hc_box *box, const int2 *nodeC, double *nm, double *ncx,
+                             double *ncy, double *ncz, double *nq, float4 *nodeA, float4 *nodeB, float4 *nodeQ)
+{
+    const int ls = box->level_start[D], le = box->level_start[D + 1];
+    const float dsqf = __double2float_rn(box->dsq[D]);
+    for (int k = ls + blockIdx.x * blockDim.x + threadIdx.x; k < le; k += gridDim.x * blockDim.x) {
+        int2 C = nodeC[k];
+        if (C.x < 0) continue;                   // body leaf
+        const int fc = C.x, nc = C.y & 255;
+        double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int i = 0; i < nc; i++) {
+            int ch = fc + i;
+            double mr = nm[ch];
+            m = dadd(m, mr);
+            cx = dadd(cx, dmul(ncx[ch], mr));
+            cy = dadd(cy, dmul(ncy[ch], mr));
+            cz = dadd(cz, dmul(ncz[ch], mr));
+        }
+        cx = ddiv(cx, m);
+        cy = ddiv(cy, m);
+        cz = ddiv(cz, m);
+        double Q[6] = {0, 0, 0, 0, 0, 0};
+        if (usequad) {
+            for (int i = 0; i < nc; i++) {
+                int ch = fc + i;
+                double mr = nm[ch];
+                double dr[3] = {dsub(ncx[ch], cx), dsub(ncy[ch], cy), dsub(ncz[ch], cz)};
+                double drsq = dmul(dr[0], dr[0]);
+                drsq = dadd(drsq, dmul(dr[1], dr[1]));
+                drsq = dadd(drsq, dmul(dr[2], dr[2]));
+                const int jj[6] = {0, 0, 0, 1, 1, 2}, kk[6] = {0, 1, 2, 1, 2, 2};
+                bool cell = nodeC[ch].x >= 0;
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    double t = dmul(dmul(dr[jj[q]], dr[kk[q]]), 3.0);
+                    if (jj[q] == kk[q]) t = dsub(t, drsq);
+                    t = dmul(t, mr);
+                    if (cell) t = dadd(t, nq[(int64_t)6 * ch + q]);
+                    Q[q] = dadd(Q[q], t);
+                }
+            }
+        }
+        nm[k] = m;
+        ncx[k] = cx;
+        ncy[k] = cy;
+        ncz[k] = cz;
+        for (int q = 0; q < 6; q++) nq[(int64_t)6 * k + q] = Q[q];
+        float4 A, B;
+        split_hilo(cx, &A.x, &B.x);
+        split_hilo(cy, &A.y, &B.y);
+        split_hilo(cz, &A.z, &B.z);
+        A.w = __double2float_rn(m);
+        B.w = dsqf;
+        nodeA[k] = A;
+        nodeB[k] = B;
+        nodeQ[2 * (int64_t)k] = make_float4(__double2float_rn(Q[0]), __double2float_rn(Q[1]),
+                                            __double2float_rn(Q[2]), __double2float_rn(Q[3]));
+        nodeQ[2 * (int64_t)k + 1] = make_float4(__double2float_rn(Q[4]), __double2float_rn(Q[5]), 0.f, 0.f);
+    }
+}
+
+__global__ void k_set_nmassive(const int32_t *total, hc_box *box) { box->nmassive = *total; }
+
+}  // namespace
+
+void hc_keys_for_points(hc_ctx *c, const double *x, const double *y, const double *z, int64_t n,
+                        unsigned long long *khi, uint32_t *klo, uint32_t *kval)
+{
+    k_keys<<<hc_grid(n, 256), 256, 0, c->stream>>>(x, y, z, n, c->box, khi, klo, kval);
+    c->launches++;
+}
+
+int hc_tree_build(hc_ctx *c)
+{
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    const int B = 256;
+    const int G = hc_grid(n, B);
+    int32_t *outside = c->flags;
+    int32_t *massive = c->flags + n;
+    int32_t *opos = c->flags + 2 * n;
+    int32_t *mrank = c->flags + 3 * n;
+
+    // 1. expandbox replay
+    k_box_flags<<<G, B, 0, s>>>(c->mass, c->px, c->py, c->pz, n, c->box, outside, massive);
+    hc_scan_exclusive_i32(c, outside, opos, n, c->ncand);
+    hc_scan_exclusive_i32(c, massive, mrank, n, nullptr);
+    k_box_compact<<<G, B, 0, s>>>(outside, opos, n, c->cand);
+    k_first_massive<<<G, B, 0, s>>>(massive, mrank, n, c->box);
+    k_box_replay<<<1, 256, 0, s>>>(c->px, c->py, c->pz, c->cand, c->ncand, mrank, c->box);
+    c->launches += 4;
+    HC_CUDA(cudaMemcpyAsync(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost, s));
+    HC_CUDA(cudaStreamSynchronize(s));
+    if (c->h_box->chain_lmin == -2) {
+        c->err = "expandbox: a massive body has a non-finite position";
+        return HC_ERR_ARG;
+    }
+
+    // 2-3. keys, sort, massive compaction
+    hc_keys_for_points(c, c->px, c->py, c->pz, n, c->khi[0], c->klo[0], c->kval[0]);
+    int sel = hc_radix_sort_keys(c, c->khi, c->klo, c->kval, n, 0, 64, true);
+    c->sort_sel = sel;
+    c->sidx = c->kval[sel];
+    int32_t *sflag = c->flags;            // reuse (outside no longer needed)
+    int32_t *srank = c->flags + n;
+    k_sorted_massive<<<G, B, 0, s>>>(c->sidx, c->mass, n, sflag);
+    hc_scan_exclusive_i32(c, sflag, srank, n, c->flags + 2 * n);
+    k_set_nmassive<<<1, 1, 0, s>>>(c->flags + 2 * n, c->box);
+    k_mcompact<<<G, B, 0, s>>>(sflag, srank, n, c->khi[sel], c->klo[sel], c->sidx, c->mhi, c->mlo, c->midx,
+                               c->mpos, c->s_rank, c->leaf_of_sorted);
+    c->launches += 3;
+
+    // 4. cells in pre-order
+    k_lcp<<<G, B, 0, s>>>(c->mhi, c->mlo, c->midx, c->box, c->dlcp, c->st);
+    // cstart lives in flags (n+1 entries); scan over n (entries beyond M are zero)
+    int32_t *cstart = c->flags + n;       // [n+1]
+    HC_CUDA(cudaMemsetAsync(c->ccount, 0, sizeof(int32_t) * (n + 1), s));
+    k_ccount<<<G, B, 0, s>>>(c->dlcp, c->midx, c->box, c->ccount);
+    hc_scan_exclusive_i32(c, c->ccount, cstart, n + 1, nullptr);
+    k_post_count<<<1, 1, 0, s>>>(cstart, c->box, c->maxcell, c->st);
+    int Gn = hc_grid(c->maxnode, B);
+    k_emit_preorder<<<G, B, 0, s>>>(c->dlcp, c->midx, cstart, c->box, c->maxnode, c->pre_info, c->pre_a,
+                                    c->dkey[0], c->dval[0]);
+    k_cell_end<<<Gn, B, 0, s>>>(c->mhi, c->mlo, c->dlcp, c->pre_info, c->pre_a, c->box, c->maxnode, c->pre_b);
+    c->launches += 6;
+
+    // Error check before the layout stage (cell overflow / coincident keys):
+    // the later kernels assume nnode <= maxnode.
+    HC_CUDA(cudaMemcpyAsync(c->h_st, c->st, sizeof(hc_status), cudaMemcpyDeviceToHost, s));
+    HC_CUDA(cudaMemcpyAsync(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost, s));
+    HC_CUDA(cudaStreamSynchronize(s));
+    if (c->h_st->error) return c->h_st->error;
+    const int nnode = c->h_box->nnode;
+    if (nnode <= 0) return HC_OK;     // no massive body: empty tree
+
+    // 5. breadth-first layout: stable sort of the pre-order by depth
+    uint32_t *nolo[2] = {nullptr, nullptr};
+    int dsel = hc_radix_sort_keys(c, c->dkey, nolo, c->dval, nnode, 0, 8, false);
+    c->bfs2pre = c->dval[dsel];
+    {
+        int nblk = (int)((nnode + 4095) / 4096);
+        k_levels<<<1, 64, 0, s>>>(c->hist, nblk, c->box);
+    }
+    int Gm = hc_grid(nnode, B);
+    k_pre2bfs<<<Gm, B, 0, s>>>(c->bfs2pre, c->box, c->pre2bfs);
+    k_parent<<<Gm, B, 0, s>>>(c->bfs2pre, c->pre_info, c->box, c->parent);
+    HC_CUDA(cudaMemsetAsync(c->nodeC, 0xff, sizeof(int2) * nnode, s));
+    HC_CUDA(cudaMemsetAsync(c->lastc, 0xff, sizeof(int32_t) * nnode, s));
+    k_children<<<Gm, B, 0, s>>>(c->parent, c->bfs2pre, c->pre_info, c->box, c->nodeC, c->lastc);
+    k_node_init<<<Gm, B, 0, s>>>(c->bfs2pre, c->pre_info, c->pre_a, c->midx, c->mpos, c->mass, c->px, c->py,
+                                 c->pz, c->box, c->nodeC, c->lastc, c->nodeA, c->nodeB, c->nodeQ, c->nm, c->ncx,
+                                 c->ncy, c->ncz, c->nq, c->leaf_of_sorted, c->st);
+    c->launches += 5;
+
+    // 6. upward pass, deepest level first
+    int Gc = hc_grid(c->maxcell > 0 ? c->maxcell : 1, B);
+    for (int D = HC_MAXLEVEL; D >= 0; D--) {
+        k_cofm_level<<<Gc, B, 0, s>>>(D, c->prm.usequad, c->box, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->nq,
+                                      c->nodeA, c->nodeB, c->nodeQ);
+        c->launches++;
+    }
+    return HC_OK;
+}
+
+// ---------------- tree dump (host assembly from device arrays) ----------------
+
+int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count, double *mass, double *cm,
+                      double *quad, int32_t *bparent)
+{
+    HC_CUDA(cudaMemcpy(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost));
+    const int M = c->h_box->nmassive, nn = c->h_box->nnode;
+    for (int64_t i = 0; i < c->n && bparent; i++) bparent[i] = -1;
+    if (nn <= 0) return 0;
+    auto H = [&](size_t bytes) { return std::unique_ptr<char[]>(new char[bytes > 0 ? bytes : 1]); };
+    auto hb = H(sizeof(uint32_t) * nn), hd = H(sizeof(int32_t) * nn), ha = H(sizeof(int32_t) * nn),
+         hbb = H(sizeof(int32_t) * nn), hmhi = H(sizeof(unsigned long long) * M), hmlo = H(sizeof(uint32_t) * M),
+         hmidx = H(sizeof(uint32_t) * M), hnm = H(sizeof(double) * nn), hx = H(sizeof(double) * nn),
+         hy = H(sizeof(double) * nn), hz = H(sizeof(double) * nn), hq = H(sizeof(double) * 6 * nn);
+    uint32_t *bfs2pre = (uint32_t *)hb.get();
+    int32_t *pd = (int32_t *)hd.get(), *pa = (int32_t *)ha.get(), *pb = (int32_t *)hbb.get();
+    unsigned long long *mhi = (unsigned long long *)hmhi.get();
+    uint32_t *mlo = (uint32_t *)hmlo.get(), *midx = (uint32_t *)hmidx.get();
+    double *nm = (double *)hnm.get(), *nx = (double *)hx.get(), *ny = (double *)hy.get(), *nz = (double *)hz.get(),
+           *nq = (double *)hq.get();
+    HC_CUDA(cudaMemcpy(bfs2pre, c->bfs2pre, sizeof(uint32_t) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(pd, c->pre_info, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(pa, c->pre_a, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(pb, c->pre_b, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(mhi, c->mhi, sizeof(unsigned long long) * M, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(mlo, c->mlo, sizeof(uint32_t) * M, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(midx, c->midx, sizeof(uint32_t) * M, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(nm, c->nm, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(nx, c->ncx, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(ny, c->ncy, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(nz, c->ncz, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(nq, c->nq, sizeof(double) * 6 * nn, cudaMemcpyDeviceToHost));
+    auto unspread = [](unsigned long long hi, uint32_t lo, int axis) {
+        // axis 0 = x (bit 2 of each digit), 1 = y, 2 = z
+        unsigned v = 0;
+        int sh = 2 - axis;
+        for (int b = 0; b < 21; b++) v |= (unsigned)((hi >> (3 * b + sh)) & 1ull) << (b + 9);
+        for (int b = 0; b < 9; b++) v |= ((lo >> (3 * b + sh)) & 1u) << b;
+        return v;
+    };
+    int ci = 0;
+    for (int k = 0; k < nn; k++) {
+        uint32_t p = bfs2pre[k];
+        int D = pd[p], a = pa[p];
+        if (a < 0) {
+            if (bparent) bparent[midx[-1 - a]] = D - 1;
+            continue;
+        }
+        if (level) level[ci] = D;
+        if (corner) {
+            for (int ax = 0; ax < 3; ax++) {
+                unsigned v = unspread(mhi[a], mlo[a], ax);
+                unsigned mask = D >= 30 ? 0xffffffffu : ~((1u << (30 - D)) - 1u);
+                corner[3 * ci + ax] = (int32_t)(v & mask);
+            }
+        }
+        if (count) count[ci] = pb[p] - a + 1;
+        if (mass) mass[ci] = nm[k];
+        if (cm) {
+            cm[3 * ci] = nx[k];
+            cm[3 * ci + 1] = ny[k];
+            cm[3 * ci + 2] = nz[k];
+        }
+        if (quad)
+            for (int q = 0; q < 6; q++) quad[6 * ci + q] = nq[(int64_t)6 * k + q];
+        ci++;
+    }
+    return ci;
+}

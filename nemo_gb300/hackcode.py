@@ -1,0 +1,383 @@
+"""Python mirror of the hackcode1 / hackforce interface over the GB300 library.
+
+The reference's interface for this path is two programs (hackcode1:
+src/nbody/evolve/hackcode/hackcode1/code.c:21-51; hackforce: hackforce.c:38-50).
+This module offers the same operations as calls, with the same keyword names,
+defaults and error behaviour, on top of the C ABI in include/hackcode_gpu.h
+(``libhackcode_gpu.so``).  There is no CPU fallback: if the CUDA library is
+missing or no GPU is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(PKG, "libhackcode_gpu.so")
+
+HC_OK = 0
+ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "cell pool exhausted", -4: "coincident bodies",
+          -5: "walk stack exhausted", -6: "call out of order", -7: "device allocation failed"}
+
+# exported symbols of include/hackcode_gpu.h
+EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_upload", "hc_set_box", "hc_get_box",
+           "hc_build_tree", "hc_tree_summary", "hc_dump_tree", "hc_forces", "hc_forces_at", "hc_download",
+           "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
+           "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_make_testdata"]
+
+
+class HCError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("tol", C.c_double), ("eps", C.c_double), ("fcells", C.c_double), ("usequad", C.c_int),
+                ("count_per_body", C.c_int)]
+
+
+class Diag(C.Structure):
+    _fields_ = [("etot", C.c_double * 3), ("keten", C.c_double * 9), ("peten", C.c_double * 9),
+                ("amten", C.c_double * 9), ("cmphase", C.c_double * 6), ("mtot", C.c_double),
+                ("n2b", C.c_int64), ("nbc", C.c_int64), ("nfcalc", C.c_int64)]
+
+
+class TreeInfo(C.Structure):
+    _fields_ = [("nbody_massive", C.c_int64), ("ncell", C.c_int64), ("max_level", C.c_int32),
+                ("rmin", C.c_double * 3), ("rsize", C.c_double)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+_lib = None
+
+
+def library(build_if_missing: bool = False) -> C.CDLL:
+    """Load libhackcode_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        if not build_if_missing:
+            raise ImportError(f"{LIBPATH} is missing: run nemo_gb300/build.py (the CUDA path has no fallback)")
+        from . import build as _b
+        _b.build()
+    L = C.CDLL(LIBPATH)
+    L.hc_create.argtypes = [C.POINTER(_vp), C.c_int64, C.POINTER(Params)]
+    L.hc_destroy.argtypes = [_vp]
+    L.hc_destroy.restype = None
+    L.hc_last_error.argtypes = [_vp]
+    L.hc_last_error.restype = C.c_char_p
+    L.hc_set_params.argtypes = [_vp, C.POINTER(Params)]
+    L.hc_upload.argtypes = [_vp, _dp, _dp]
+    L.hc_set_box.argtypes = [_vp, _dp, C.c_double]
+    L.hc_get_box.argtypes = [_vp, _dp, C.POINTER(C.c_double)]
+    L.hc_build_tree.argtypes = [_vp]
+    L.hc_tree_summary.argtypes = [_vp, C.POINTER(TreeInfo)]
+    L.hc_dump_tree.argtypes = [_vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]
+    L.hc_forces.argtypes = [_vp]
+    L.hc_forces_at.argtypes = [_vp, _dp, C.c_int64, _dp, _dp]
+    L.hc_download.argtypes = [_vp, _vp, _vp, _vp]
+    L.hc_body_counts.argtypes = [_vp, _ip, _ip]
+    L.hc_step.argtypes = [_vp, C.c_double, C.c_int64, C.POINTER(Diag), _vp, _vp, _vp]
+    L.hc_diagnostics.argtypes = [_vp, C.POINTER(Diag)]
+    L.hc_direct_sample.argtypes = [_vp, _lp, C.c_int64, _dp, _dp]
+    L.hc_last_timing.argtypes = [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    L.hc_timer_start.argtypes = [_vp]
+    L.hc_timer_stop.argtypes = [_vp, C.POINTER(C.c_double)]
+    L.hc_fp32_peak.argtypes = [_vp, C.POINTER(C.c_double)]
+    L.hc_mkplummer.argtypes = [C.c_int, C.c_int, _dp, _dp]
+    L.hc_mkplummer.restype = None
+    L.hc_make_testdata.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
+    L.hc_make_testdata.restype = None
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One system of nbody bodies on the GPU (one CUDA stream, all memory owned)."""
+
+    def __init__(self, nbody: int, tol: float = 1.0, eps: float = 0.05, fcells: float = 1.0,
+                 usequad: bool = False, count_per_body: bool = False):
+        self._L = library()
+        self.n = int(nbody)
+        self.params = Params(float(tol), float(eps), float(fcells), int(bool(usequad)), int(bool(count_per_body)))
+        h = _vp()
+        rc = self._L.hc_create(C.byref(h), self.n, C.byref(self.params))
+        self._h = h
+        if rc != HC_OK:
+            msg = self._L.hc_last_error(h).decode() if h.value else "hc_create failed"
+            self.close()
+            raise HCError(rc, msg)
+
+    def _check(self, rc: int):
+        if rc != HC_OK:
+            raise HCError(rc, self._L.hc_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.hc_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- state ----
+    def set_params(self, **kw):
+        for k, v in kw.items():
+            setattr(self.params, k, type(getattr(self.params, k))(v))
+        self._check(self._L.hc_set_params(self._h, C.byref(self.params)))
+
+    def upload(self, mass, phase):
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        ph = np.ascontiguousarray(phase, dtype=np.float64).reshape(-1, 2, 3)
+        if len(m) != self.n or len(ph) != self.n:
+            raise ValueError("mass/phase length must equal nbody")
+        if not (np.isfinite(m).all() and np.isfinite(ph).all()):
+            raise ValueError("non-finite mass or phase-space coordinates")
+        self._check(self._L.hc_upload(self._h, m, ph))
+
+    def upload_ptr(self, mass_ptr: int, phase_ptr: int):
+        """Upload from raw host pointers (e.g. pinned buffers): Mass[n], PhaseSpace[n][2][3]."""
+        raw = self._L["hc_upload"]          # a second handle with pointer-typed arguments
+        raw.argtypes = [_vp, _vp, _vp]
+        self._check(raw(self._h, mass_ptr, phase_ptr))
+
+    def download_ptr(self, phase_ptr=None, acc_ptr=None, phi_ptr=None):
+        """Download to raw host pointers (any may be None)."""
+        self._check(self._L.hc_download(self._h, phase_ptr, acc_ptr, phi_ptr))
+
+    def timer_start(self):
+        self._check(self._L.hc_timer_start(self._h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._check(self._L.hc_timer_stop(self._h, C.byref(ms)))
+        return ms.value
+
+    def fp32_peak_tflops(self) -> float:
+        t = C.c_double()
+        self._check(self._L.hc_fp32_peak(self._h, C.byref(t)))
+        return t.value
+
+    def set_box(self, rmin, rsize):
+        self._check(self._L.hc_set_box(self._h, np.ascontiguousarray(rmin, dtype=np.float64), float(rsize)))
+
+    def box(self):
+        r = np.zeros(3)
+        s = C.c_double()
+        self._check(self._L.hc_get_box(self._h, r, C.byref(s)))
+        return r, s.value
+
+    # ---- tree / forces ----
+    def build_tree(self):
+        self._check(self._L.hc_build_tree(self._h))
+
+    def tree_info(self) -> TreeInfo:
+        t = TreeInfo()
+        self._check(self._L.hc_tree_summary(self._h, C.byref(t)))
+        return t
+
+    def dump_tree(self):
+        t = self.tree_info()
+        nc = int(t.ncell)
+        d = dict(level=np.zeros(nc, np.int32), corner=np.zeros((nc, 3), np.int32), count=np.zeros(nc, np.int32),
+                 mass=np.zeros(nc), cm=np.zeros((nc, 3)), quad=np.zeros((nc, 6)),
+                 body_parent_level=np.zeros(self.n, np.int32))
+        self._check(self._L.hc_dump_tree(self._h, d["level"], d["corner"], d["count"], d["mass"], d["cm"],
+                                         d["quad"], d["body_parent_level"]))
+        return d
+
+    def forces(self):
+        self._check(self._L.hc_forces(self._h))
+
+    def forces_at(self, test_pos):
+        tp = np.ascontiguousarray(test_pos, dtype=np.float64).reshape(-1, 3)
+        acc = np.zeros((len(tp), 3))
+        phi = np.zeros(len(tp))
+        self._check(self._L.hc_forces_at(self._h, tp, len(tp), acc, phi))
+        return acc, phi
+
+    def download(self, phase=True, acc=True, phi=True):
+        ph = np.zeros((self.n, 2, 3)) if phase else None
+        a = np.zeros((self.n, 3)) if acc else None
+        p = np.zeros(self.n) if phi else None
+        self._check(self._L.hc_download(self._h, _ptr(ph), _ptr(a), _ptr(p)))
+        return ph, a, p
+
+    def body_counts(self):
+        b = np.zeros(self.n, np.int32)
+        c = np.zeros(self.n, np.int32)
+        self._check(self._L.hc_body_counts(self._h, b, c))
+        return b, c
+
+    def diagnostics(self) -> Diag:
+        d = Diag()
+        self._check(self._L.hc_diagnostics(self._h, C.byref(d)))
+        return d
+
+    def step(self, dt: float, nstep: int, snapshot: bool = False):
+        d = Diag()
+        ph = a = p = None
+        if snapshot:
+            ph, a, p = np.zeros((self.n, 2, 3)), np.zeros((self.n, 3)), np.zeros(self.n)
+        self._check(self._L.hc_step(self._h, float(dt), int(nstep), C.byref(d), _ptr(ph), _ptr(a), _ptr(p)))
+        return d, ph, a, p
+
+    def direct_sample(self, index):
+        idx = np.ascontiguousarray(index, dtype=np.int64)
+        acc = np.zeros((len(idx), 3))
+        phi = np.zeros(len(idx))
+        self._check(self._L.hc_direct_sample(self._h, idx, len(idx), acc, phi))
+        return acc, phi
+
+    def timing(self):
+        b, w, n = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self._L.hc_last_timing(self._h, C.byref(b), C.byref(w), C.byref(n)))
+        return b.value, w.value, n.value
+
+
+# ---------------------------------------------------------------- tool-level calls
+
+def mkplummer(n: int, seed: int = 0):
+    """Plummer model as mkplummer draws it with default keywords: (mass[n], phase[n,2,3])."""
+    m = np.zeros(n)
+    ph = np.zeros((n, 2, 3))
+    library().hc_mkplummer(int(n), int(seed), m, ph)
+    return m, ph
+
+
+def make_testdata(n: int, seed: int = 123, cencon: bool = False):
+    """hackcode1's nbody= initial conditions: (mass[n], phase[n,2,3])."""
+    m = np.zeros(n)
+    ph = np.zeros((n, 2, 3))
+    library().hc_make_testdata(int(n), int(seed), int(bool(cencon)), m, ph)
+    return m, ph
+
+
+def hackforce(mass, pos, test=None, tol=1.0, eps=0.05, rsize=4.0, rmin=None, fcells=0.75, usequad=False):
+    """One force evaluation with hackforce semantics (hackforce.c:177-215).
+
+    The tree holds the massive bodies of (mass, pos); forces are returned at
+    every body (its own body skipped) or, with test=, at the test positions
+    (nothing skipped).  Returns (acc, phi, n2btot, nbctot) with 64-bit counts.
+    """
+    mass = np.ascontiguousarray(mass, dtype=np.float64)
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    n = len(mass)
+    if n < 1:
+        raise ValueError("read_snapshot: Nobj < 1 is absurd")
+    if rmin is None:
+        rmin = np.full(3, -rsize / 2.0)
+    phase = np.zeros((n, 2, 3))
+    phase[:, 0] = pos
+    with Context(n, tol=tol, eps=eps, fcells=fcells, usequad=usequad) as ctx:
+        ctx.upload(mass, phase)
+        ctx.set_box(rmin, rsize)
+        ctx.build_tree()
+        if test is None:
+            ctx.forces()
+            _, acc, phi = ctx.download(phase=False)
+            d = ctx.diagnostics()
+            return acc, phi, int(d.n2b), int(d.nbc)
+        acc, phi = ctx.forces_at(test)
+        d = ctx.diagnostics()
+        return acc, phi, int(d.n2b), int(d.nbc)
+
+
+@dataclass
+class LogRow:
+    """One block of hackcode1's log (code_io.c:119-129)."""
+    tnow: float
+    etot: tuple
+    nttot: int
+    nbavg: int
+    ncavg: int
+    cmphase: tuple
+    n2b: int = 0
+    nbc: int = 0
+
+
+@dataclass
+class RunResult:
+    phase: np.ndarray
+    acc: np.ndarray
+    phi: np.ndarray
+    rows: list = field(default_factory=list)
+    snapshots: list = field(default_factory=list)   # (tnow, bits, mass, phase, phi, acc, diag)
+    box: tuple = None
+
+
+TIME_BIT, PHASE_BIT, MASS_BIT, PHI_BIT, ACC_BIT = 1, 2, 4, 8, 16
+
+
+def hackcode1(mass, phase, tnow=0.0, freq=32.0, eps=0.05, tol=1.0, fcells=1.0, tstop=2.0, freqout=4.0,
+              minor_freqout=32.0, options="mass,phase", usequad=False, keep_snapshots=True, on_output=None):
+    """Integrate with hackcode1 semantics (code.c:57-64,159-191; code_io.c:111-154).
+
+    Each step builds the tree, evaluates forces with the closing half-kick,
+    records the log row and any due snapshot, then kicks and drifts.  The
+    snapshot list holds what hackcode1 would write to out= (or on_output is
+    called with each one)."""
+    mass = np.ascontiguousarray(mass, dtype=np.float64)
+    phase = np.ascontiguousarray(phase, dtype=np.float64).reshape(-1, 2, 3)
+    n = len(mass)
+    opts = [w.strip() for w in options.split(",")]
+    res = RunResult(phase=None, acc=None, phi=None)
+    tout = minor_tout = tnow
+    nstep = 0
+    firstmass = True
+    with Context(n, tol=tol, eps=eps, fcells=fcells, usequad=usequad) as ctx:
+        ctx.upload(mass, phase)
+        while tnow < tstop + 0.1 / freq:
+            dt = 1.0 / freq
+            bits = 0
+            if minor_freqout > 0.0 and (minor_tout - 0.01 / freq) <= tnow:
+                minor_tout += 1.0 / minor_freqout
+                bits |= TIME_BIT
+            if freqout > 0.0 and (tout - 0.01 / freq) <= tnow:
+                tout += 1.0 / freqout
+                bits |= TIME_BIT | PHASE_BIT
+                if "mass" in opts or firstmass:
+                    bits |= MASS_BIT
+                    firstmass = False
+                if "phi" in opts:
+                    bits |= PHI_BIT
+                if "acc" in opts:
+                    bits |= ACC_BIT
+            need = bool(bits & (PHASE_BIT | PHI_BIT | ACC_BIT))
+            d, ph, a, p = ctx.step(dt, nstep, snapshot=need)
+            nf = max(int(d.nfcalc), 1)
+            res.rows.append(LogRow(tnow, tuple(d.etot), int(d.n2b + d.nbc), int(d.n2b / nf), int(d.nbc / nf),
+                                   tuple(d.cmphase), int(d.n2b), int(d.nbc)))
+            if bits:
+                snap = (tnow, bits, mass, ph, p, a, d)
+                if on_output:
+                    on_output(snap)
+                if keep_snapshots:
+                    res.snapshots.append(snap)
+            nstep += 1
+            tnow = tnow + dt
+        res.phase, res.acc, res.phi = ctx.download()
+        res.box = ctx.box()
+    return res

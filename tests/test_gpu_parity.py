@@ -1,0 +1,224 @@
+"""GPU parity: the CUDA path against the reference (fixtures) and the oracle.
+
+Checks, per the hot-path contract:
+  (a) the octree cell set, per-cell body counts, body membership and FP64
+      moments are bit-identical to the reference maketree/hackcofm;
+  (b) per-body interaction counts are identical and accelerations /
+      potentials agree to 1e-5 relative on at least 99.9% of bodies;
+  (c) force errors against an FP64 direct sum are stated;
+  (d) energy drift of a hackcode1 run stays within 10% of the reference's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5        # per-body relative tolerance of (b)
+FRACTION = 0.999      # fraction of bodies that must meet it
+
+
+@pytest.fixture(scope="module")
+def hc():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from nemo_gb300 import build as B
+    B.build()
+    from nemo_gb300 import hackcode
+    return hackcode
+
+
+def _canon(d):
+    k = np.lexsort((d["corner"][:, 2], d["corner"][:, 1], d["corner"][:, 0], d["level"]))
+    return {f: d[f][k] for f in ("level", "corner", "count", "mass", "cm", "quad")}
+
+
+def _golden(case):
+    return np.load(os.path.join(HERE, "golden", case + ".npz"))
+
+
+def _rel_err(a, b):
+    """|a - b| / |b| per body (vectors) or per value."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if a.ndim == 2:
+        return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+
+def _ctx_for(hc, g, quad, count=True):
+    m, pos = g["mass"], g["pos"]
+    ph = np.zeros((len(m), 2, 3))
+    ph[:, 0] = pos
+    ctx = hc.Context(len(m), tol=float(g["tol"]), eps=float(g["eps"]), fcells=1.0, usequad=quad,
+                     count_per_body=count)
+    ctx.upload(m, ph)
+    ctx.build_tree()
+    return ctx
+
+
+@pytest.mark.parametrize("case", ["plummer4096_s123", "testdata128_s123", "plummer2048_s7_test"])
+@pytest.mark.parametrize("quad", [False, True])
+def test_tree_bit_exact_vs_reference(hc, case, quad):
+    g = _golden(case)
+    tag = "qp" if quad else "mp"
+    with _ctx_for(hc, g, quad) as ctx:
+        rmin, rsize = ctx.box()
+        assert np.array_equal(rmin, g[f"{tag}_rmin"]) and rsize == float(g[f"{tag}_rsize"])
+        d = ctx.dump_tree()
+        c = _canon(d)
+        assert len(c["level"]) == len(g[f"{tag}_cell_level"])
+        for f in ("level", "corner", "count", "mass", "cm", "quad"):
+            assert np.array_equal(c[f], g[f"{tag}_cell_{f}"]), f
+        assert np.array_equal(d["body_parent_level"], g[f"{tag}_body_parent_level"])
+
+
+@pytest.mark.parametrize("case", ["plummer4096_s123", "testdata128_s123"])
+@pytest.mark.parametrize("quad", [False, True])
+def test_forces_match_reference(hc, case, quad):
+    g = _golden(case)
+    tag = "qp" if quad else "mp"
+    with _ctx_for(hc, g, quad) as ctx:
+        ctx.forces()
+        _, acc, phi = ctx.download(phase=False)
+        n2b, nbc = ctx.body_counts()
+        d = ctx.diagnostics()
+    # identical interaction sets: every per-body count equals the reference's
+    assert np.array_equal(n2b, g[f"{tag}_n2b"]) and np.array_equal(nbc, g[f"{tag}_nbc"])
+    assert d.n2b == int(g[f"{tag}_n2b"].sum()) and d.nbc == int(g[f"{tag}_nbc"].sum())
+    ea = _rel_err(acc, g[f"{tag}_acc"])
+    ep = _rel_err(phi, g[f"{tag}_phi"])
+    ok = (ea <= REL_TOL) & (ep <= REL_TOL)
+    assert ok.mean() >= FRACTION, (ok.mean(), np.sort(ea)[-5:], np.sort(ep)[-5:])
+    assert np.isfinite(acc).all() and np.isfinite(phi).all()
+
+
+@pytest.mark.parametrize("quad", [False, True])
+def test_forces_at_test_points(hc, quad):
+    g = _golden("plummer2048_s7_test")
+    tag = "qp" if quad else "mp"
+    with _ctx_for(hc, g, quad, count=False) as ctx:
+        acc, phi = ctx.forces_at(g["test_pos"])
+        d = ctx.diagnostics()
+    assert d.n2b == int(g[f"{tag}_n2b"].sum()) and d.nbc == int(g[f"{tag}_nbc"].sum())
+    ok = (_rel_err(acc, g[f"{tag}_acc"]) <= REL_TOL) & (_rel_err(phi, g[f"{tag}_phi"]) <= REL_TOL)
+    assert ok.mean() >= FRACTION
+
+
+def test_expansion_chain_and_massless(hc, oracle_lib):
+    """One-body expansion cells (load.c:74-93) and massless test bodies."""
+    O = oracle_lib
+    far = np.array([[0.1, 0.2, 0.3], [40.0, -70.0, 15.0], [45.0, -65.0, 18.0], [38.0, -71.0, 12.0],
+                    [0.5, -0.4, 0.2], [41.0, -69.0, 14.0]])
+    m = np.array([0.25, 0.25, 0.25, 0.25, 0.0, 0.0])      # last two massless
+    for quad in (False, True):
+        T = O.Tree(len(m), 4.0)
+        assert T.build(m, far, quad) == 0
+        ref = _canon(T.dump())
+        ra, rp, rb, rc = T.forces(0.6, 0.02, quad)
+        ph = np.zeros((len(m), 2, 3))
+        ph[:, 0] = far
+        with hc.Context(len(m), tol=0.6, eps=0.02, fcells=4.0, usequad=quad, count_per_body=True) as ctx:
+            ctx.upload(m, ph)
+            ctx.build_tree()
+            got = _canon(ctx.dump_tree())
+            for f in ref:
+                assert np.array_equal(got[f], ref[f]), f
+            assert (got["count"] == 1).any()
+            ctx.forces()
+            _, acc, phi = ctx.download(phase=False)
+            b, c = ctx.body_counts()
+        assert np.array_equal(b, rb) and np.array_equal(c, rc)
+        assert np.allclose(acc, ra, rtol=1e-5, atol=1e-12) and np.allclose(phi, rp, rtol=1e-5)
+
+
+def test_errors_are_reported(hc, oracle_lib):
+    m, ph = oracle_lib.mkplummer(512, 9)
+    with hc.Context(512, fcells=0.1) as ctx:
+        ctx.upload(m, ph)
+        with pytest.raises(hc.HCError) as e:
+            ctx.build_tree()
+        assert e.value.code == -3 and "increase fcells" in str(e.value)
+    ph2 = ph.copy()
+    ph2[3, 0] = ph2[7, 0]
+    with hc.Context(512) as ctx:
+        ctx.upload(m, ph2)
+        with pytest.raises(hc.HCError) as e:
+            ctx.build_tree()
+        assert e.value.code == -4
+    with hc.Context(512) as ctx:
+        ctx.upload(m, ph)
+        with pytest.raises(hc.HCError) as e:
+            ctx.forces()
+        assert e.value.code == -6
+
+
+def test_single_and_empty_trees(hc):
+    ph = np.zeros((3, 2, 3))
+    ph[:, 0] = [[0.1, 0.0, 0.0], [0.5, 0.2, -0.3], [-0.4, 0.1, 0.9]]
+    m = np.array([1.0, 0.0, 0.0])                     # one massive body: the root is a body
+    with hc.Context(3, tol=1.0, eps=0.05) as ctx:
+        ctx.upload(m, ph)
+        ctx.build_tree()
+        ctx.forces()
+        _, acc, phi = ctx.download(phase=False)
+    assert acc[0].tolist() == [0.0, 0.0, 0.0] and phi[0] == 0.0
+    dr = ph[0, 0] - ph[1, 0]
+    r2 = dr @ dr + 0.05 ** 2
+    assert np.allclose(phi[1], -1.0 / np.sqrt(r2), rtol=1e-6)
+    assert np.allclose(acc[1], dr / r2 ** 1.5, rtol=1e-5)
+
+
+def test_direct_sample_and_force_error(hc, oracle_lib):
+    O = oracle_lib
+    m, ph = O.mkplummer(4096, 123)
+    pos = ph[:, 0].copy()
+    idx = np.arange(0, 4096, 7, dtype=np.int64)
+    ea, ep = O.direct(m, pos, test_pos=pos[idx], eps=0.05, skip=idx.astype(np.int32))
+    with hc.Context(4096, tol=0.7, eps=0.05, usequad=True) as ctx:
+        ctx.upload(m, ph)
+        ctx.build_tree()
+        ga, gp = ctx.direct_sample(idx)
+        ctx.forces()
+        _, acc, phi = ctx.download(phase=False)
+    assert np.allclose(ga, ea, rtol=1e-10, atol=1e-13) and np.allclose(gp, ep, rtol=1e-10)
+    err = _rel_err(acc[idx], ea)
+    rms = float(np.sqrt(np.mean(err ** 2)))
+    p99 = float(np.percentile(err, 99))
+    print(f"tol=0.7 quad force error vs FP64 direct sum: rms {rms:.3e} p99 {p99:.3e}")
+    assert rms < 5e-3 and p99 < 2e-2
+
+
+def test_hackcode1_run_energy_and_log(hc, oracle_lib):
+    """Config-1 shape (N=4096 Plummer, tol=0.7, eps=0.05, dt=1/32) for 16
+    steps: log counts identical to the oracle each step; energy drift within
+    10% of the oracle's (plus a floor of 1e-6 of |E|)."""
+    O = oracle_lib
+    m, ph = O.mkplummer(4096, 123)
+    kw = dict(freq=32.0, eps=0.05, tol=0.7, tstop=0.5, freqout=2.0, minor_freqout=2.0)
+    _, _, _, rows, _, box = O.hackcode1(m, ph, write_out=False, **kw)
+    res = hc.hackcode1(m, ph, options="mass,phi,acc", keep_snapshots=False, **kw)
+    assert len(res.rows) == len(rows)
+    for rg, ro in zip(res.rows, rows):
+        assert rg.nttot == ro.nttot and rg.nbavg == ro.nbavg and rg.ncavg == ro.ncavg
+    e0, e1 = rows[0].etot[0], rows[-1].etot[0]
+    g0, g1 = res.rows[0].etot[0], res.rows[-1].etot[0]
+    assert abs((g1 - g0) - (e1 - e0)) <= 0.1 * abs(e1 - e0) + 1e-6 * abs(e0)
+    assert np.array_equal(res.box[0], box[0]) and res.box[1] == box[1]
+
+
+def test_hackcode1_testfile_fingerprint(hc, oracle_lib):
+    """The hackcode1 Testfile run (nbody=128, defaults) through the GPU path:
+    log counts identical to the reference's man-page values."""
+    import json
+    pins = json.load(open(os.path.join(HERE, "golden", "reference_pins.json")))
+    m, ph = oracle_lib.make_testdata(128, 123)
+    res = hc.hackcode1(m, ph)
+    first, last = res.rows[0], res.rows[-1]
+    for row, key in ((first, "manpage_first"), (last, "manpage_last")):
+        pin = pins[key]
+        assert (row.nttot, row.nbavg, row.ncavg) == (pin["nttot"], pin["nbavg"], pin["ncavg"])
+        assert "%.4f" % row.etot[0] == "%.4f" % pin["T+U"]
