@@ -84,6 +84,11 @@ int hc_set_params(hc_ctx *ctx, const hc_params *params);
  * Replaces: inputdata / get_snap body fill, code_io.c:35-56. */
 int hc_upload(hc_ctx *ctx, const double *mass, const double *phase);
 
+/* Restore Acceleration[n][3] and Potential[n] of a saved state (restart=,
+ * code_io.c:254-284): the next hc_step's closing half-kick uses them as the
+ * old accelerations.  Either pointer may be NULL. */
+int hc_set_forces(hc_ctx *ctx, const double *acc, const double *phi);
+
 /* Root box (rmin, rsize); starts at (-2,-2,-2), 4 (code.c:119-120) and only
  * grows (expandbox, load.c:68-95). */
 int hc_set_box(hc_ctx *ctx, const double rmin[3], double rsize);
@@ -142,6 +147,16 @@ int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t nsample, double 
  * the context stream) and kernel launch count of the last call. */
 int hc_last_timing(hc_ctx *ctx, double *build_ms, double *walk_ms, int64_t *launches);
 
+/* Walk statistics of the last force evaluation: candidates classified,
+ * candidates needing the per-body test, interaction-list entries evaluated
+ * (bodies, cells; 32 lanes each), borderline decisions re-done in FP64 and the
+ * deepest traversal stack. */
+typedef struct {
+    int64_t candidates, mixed, entries_body, entries_cell, borderline, max_stack;
+    int64_t mask_hist[33];   /* entries by accept-mask popcount (only with count_per_body) */
+} hc_walk_stats;
+int hc_walk_statistics(hc_ctx *ctx, hc_walk_stats *out);
+
 /* Device timers on the context stream (CUDA events): start, then stop
  * returns the elapsed milliseconds; both bracket whatever was launched on the
  * context between them. */
@@ -157,6 +172,13 @@ int hc_fp32_peak(hc_ctx *ctx, double *tflops);
  * and hackcode1's nbody= test data (hackcode1/code.c:129-153). */
 void hc_mkplummer(int n, int seed, double *mass, double *phase);
 void hc_make_testdata(int n, int seed, int cencon, double *mass, double *phase);
+
+/* Host services of the drop-in programs, exported for tests: copy every
+ * snapshot of a filestruct file through the reader and writer (returns the
+ * snapshot count or -1), and evaluate a keyword expression as getdparam does
+ * (src/kernel/io/getparam.c). */
+int hc_snapcopy(const char *in, const char *out);
+double hc_nemo_eval(const char *expr, int *ok);
 
 #ifdef __cplusplus
 }

@@ -295,6 +295,22 @@ int hc_upload(hc_ctx *ctx, const double *mass, const double *phase)
     return HC_OK;
 }
 
+int hc_set_forces(hc_ctx *ctx, const double *acc, const double *phi)
+{
+    if (!ctx) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    const int64_t n = c->n;
+    if (acc) {
+        HC_TRY(staging(c, c->stage, 6 * n));
+        HC_CUDA(cudaMemcpyAsync(c->stage.d, acc, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+        k_unpack3<<<hc_grid(n, 256), 256, 0, c->stream>>>(c->stage.d, n, c->ax, c->ay, c->az);
+    }
+    if (phi) HC_CUDA(cudaMemcpyAsync(c->phi, phi, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
 int hc_set_box(hc_ctx *c, const double rmin[3], double rsize)
 {
     if (!c || !rmin || !(rsize > 0)) return HC_ERR_ARG;
@@ -525,6 +541,21 @@ int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t ns, double *acc,
     HC_CUDA(cudaMemcpyAsync(phi, c->d_out + 3 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));
     HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int hc_walk_statistics(hc_ctx *c, hc_walk_stats *o)
+{
+    if (!c || !o) return HC_ERR_ARG;
+    HC_CUDA(cudaMemcpyAsync(c->h_st, c->st, sizeof(hc_status), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    o->candidates = (int64_t)c->h_st->ncand;
+    o->mixed = (int64_t)c->h_st->nmixed;
+    o->entries_body = (int64_t)c->h_st->nentry_b;
+    o->entries_cell = (int64_t)c->h_st->nentry_c;
+    o->borderline = c->h_st->nborder;
+    o->max_stack = c->h_st->max_stack;
+    for (int i = 0; i < 33; i++) o->mask_hist[i] = (int64_t)c->h_st->mask_hist[i];
     return HC_OK;
 }
 

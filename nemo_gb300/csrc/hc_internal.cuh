@@ -28,6 +28,11 @@ struct hc_status {
     unsigned long long nbc;
     int max_stack;            // deepest walk stack seen
     int nborder;              // borderline opening decisions re-done in FP64
+    unsigned long long ncand;     // candidate nodes classified by the walk
+    unsigned long long nmixed;    // ... that needed the per-body test
+    unsigned long long nentry_b;  // body-list entries evaluated (32 lanes each)
+    unsigned long long nentry_c;  // cell-list entries evaluated
+    unsigned long long mask_hist[33];  // entries by accept-mask popcount (counting walk only)
 };
 
 // Root box state, kept on the device so the whole step can run without a

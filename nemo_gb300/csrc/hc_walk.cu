@@ -37,7 +37,7 @@
 namespace {
 
 constexpr int WARPS = 4;        // warps per block
-constexpr int STACK = 768;      // traversal stack entries per warp
+constexpr int STACK = 256;      // traversal stack entries per warp (deepest seen at N=1M: 136)
 constexpr int BCAP = 64;        // body interaction list entries per warp
 constexpr int CCAP = 64;        // cell interaction list entries per warp
 constexpr unsigned FULL = 0xffffffffu;
@@ -123,6 +123,38 @@ __device__ __forceinline__ bool open_exact(double cx, double cy, double cz, doub
     return __dmul_rn(tol2, d2) < dsq;
 }
 
+// gravsub (grav.c:42-73) for one cell in group-relative FP32; `on` = this
+// lane's body takes the interaction.  Accumulates into the chunk partials.
+template <bool QUAD>
+__device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const float qyz, const float qzz, bool on,
+                                          float bx, float by, float bz, float eps2, float &pphi, float &pax,
+                                          float &pay, float &paz)
+{
+    const float dx = P.x - bx, dy = P.y - by, dz = P.z - bz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    const float rinv = rsqrtf(r2);
+    const float rinv2 = rinv * rinv;
+    const float mr = on ? P.w * rinv : 0.f;
+    const float mr3 = mr * rinv2;
+    pphi -= mr;
+    pax = fmaf(mr3, dx, pax);
+    pay = fmaf(mr3, dy, pay);
+    paz = fmaf(mr3, dz, paz);
+    if (QUAD) {
+        const float qx = fmaf(Q0.x, dx, fmaf(Q0.y, dy, Q0.z * dz));
+        const float qy = fmaf(Q0.y, dx, fmaf(Q0.w, dy, qyz * dz));
+        const float qz = fmaf(Q0.z, dx, fmaf(qyz, dy, qzz * dz));
+        const float dqd = fmaf(qx, dx, fmaf(qy, dy, qz * dz));
+        const float r5 = on ? rinv2 * rinv2 * rinv : 0.f;
+        const float t = dqd * r5;                 // dr.Q.dr / r^5
+        pphi = fmaf(-0.5f, t, pphi);              // phiquad = -t/2
+        const float sq = 2.5f * t * rinv2;        // -5 phiquad / r^2
+        pax = fmaf(sq, dx, fmaf(-r5, qx, pax));
+        pay = fmaf(sq, dy, fmaf(-r5, qy, pay));
+        paz = fmaf(sq, dz, fmaf(-r5, qz, paz));
+    }
+}
+
 template <bool QUAD, bool COUNT>
 __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
 {
@@ -133,7 +165,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
     const int64_t ngroups = (g.ntarget + 31) / 32;
     const int nnode = g.box->nnode;
     const float tol2 = g.tol2f, eps2 = g.eps2f;
-    unsigned long long tot_b = 0, tot_c = 0;
+    unsigned long long tot_b = 0, tot_c = 0, st_cand = 0, st_mixed = 0, st_eb = 0, st_ec = 0;
     int max_sp = 0, nborder = 0;
 
     while (true) {
@@ -177,6 +209,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
         int myb = 0, myc = 0;                              // per-body counts
 
         auto flush_bodies = [&](int nb) {
+            st_eb += nb;
             float pphi = 0.f, pax = 0.f, pay = 0.f, paz = 0.f;
             for (int e = 0; e < nb; e++) {
                 const float4 P = S.bl[e];
@@ -200,36 +233,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
             kahan_add(saz, caz, paz);
         };
         auto flush_cells = [&](int nc) {
+            st_ec += nc;
             float pphi = 0.f, pax = 0.f, pay = 0.f, paz = 0.f;
             for (int e = 0; e < nc; e++) {
                 const float4 P = S.cl[e];
                 const float4 Q1 = S.cq1[e];
-                const unsigned m = __float_as_uint(Q1.z);
-                const bool bit = (m >> lane) & 1u;
-                const float dx = P.x - bx, dy = P.y - by, dz = P.z - bz;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                const float rinv = rsqrtf(r2);
-                const float rinv2 = rinv * rinv;
-                const float mr = bit ? P.w * rinv : 0.f;
-                const float mr3 = mr * rinv2;
-                pphi -= mr;
-                pax = fmaf(mr3, dx, pax);
-                pay = fmaf(mr3, dy, pay);
-                paz = fmaf(mr3, dz, paz);
-                if (QUAD) {
-                    const float4 Q0 = S.cq0[e];
-                    const float qx = fmaf(Q0.x, dx, fmaf(Q0.y, dy, Q0.z * dz));
-                    const float qy = fmaf(Q0.y, dx, fmaf(Q0.w, dy, Q1.x * dz));
-                    const float qz = fmaf(Q0.z, dx, fmaf(Q1.x, dy, Q1.y * dz));
-                    const float dqd = fmaf(qx, dx, fmaf(qy, dy, qz * dz));
-                    const float r5 = bit ? rinv2 * rinv2 * rinv : 0.f;
-                    const float t = dqd * r5;                 // dr.Q.dr / r^5
-                    pphi = fmaf(-0.5f, t, pphi);              // phiquad = -t/2
-                    const float sq = 2.5f * t * rinv2;        // -5 phiquad / r^2
-                    pax = fmaf(sq, dx, fmaf(-r5, qx, pax));
-                    pay = fmaf(sq, dy, fmaf(-r5, qy, pay));
-                    paz = fmaf(sq, dz, fmaf(-r5, qz, paz));
-                }
+                const bool bit = (__float_as_uint(Q1.z) >> lane) & 1u;
+                const float4 Q0 = QUAD ? S.cq0[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+                cell_term<QUAD>(P, Q0, Q1.x, Q1.y, bit, bx, by, bz, eps2, pphi, pax, pay, paz);
                 if (COUNT) myc += bit;
             }
             kahan_add(sphi, cphi, pphi);
@@ -300,6 +311,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
                 }
             }
             unsigned mixedb = __ballot_sync(FULL, mixed);
+            st_cand += ncand;
+            st_mixed += __popc(mixedb);
             while (mixedb) {
                 const int j = __ffs(mixedb) - 1;
                 mixedb &= mixedb - 1;
@@ -341,6 +354,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
 
             // ---- append accepted nodes to the interaction lists ----
             const bool ab = accm != 0u && isbody, ac = accm != 0u && !isbody;
+            if (COUNT && accm != 0u) atomicAdd(&g.st->mask_hist[__popc(accm)], 1ull);
             const unsigned bbal = __ballot_sync(FULL, ab), cbal = __ballot_sync(FULL, ac);
             if (ab) {
                 // node - centre as an unevaluated float sum hi + lo (TwoSum of the hi parts)
@@ -421,6 +435,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
         atomicAdd(&g.st->nbc, tot_c);
         atomicMax(&g.st->max_stack, max_sp);
         atomicAdd(&g.st->nborder, nborder);
+        atomicAdd(&g.st->ncand, st_cand);
+        atomicAdd(&g.st->nmixed, st_mixed);
+        atomicAdd(&g.st->nentry_b, st_eb);
+        atomicAdd(&g.st->nentry_c, st_ec);
     }
 }
 

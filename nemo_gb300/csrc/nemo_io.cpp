@@ -625,8 +625,65 @@ double cputime_minutes()
 
 }  // namespace nemo
 
+using nemo::Expr;
+
 // ---- C entry points for the generators (used by bench.py and the tests)
 extern "C" {
+// snapcopy: read every snapshot of `in` (with its history) and write it to
+// `out` in canonical layout.  Returns the number of snapshots or -1.
+int hc_snapcopy(const char *in, const char *out)
+{
+    try {
+        FILE *fi = nemo::stropen(in, "r");
+        nemo::Reader r(fi);
+        FILE *fo = nemo::stropen(out, "w");
+        nemo::Writer w(fo);
+        std::vector<std::string> hist;
+        std::string head;
+        nemo::Snapshot s;
+        int count = 0;
+        while (nemo::read_snapshot(r, s, &hist, &head)) {
+            if (count == 0) nemo::write_history(w, hist, head);
+            w.set("SnapShot");
+            w.set("Parameters");
+            w.data("Nobj", "i", &s.nbody, 4, {});
+            if (s.bits & nemo::TimeBit) w.data("Time", "d", &s.time, 8, {});
+            w.tes("Parameters");
+            w.set("Particles");
+            int cs = nemo::CS_CARTESIAN_3_2;
+            w.data("CoordSystem", "i", &cs, 4, {});
+            if (s.bits & nemo::MassBit) w.data("Mass", "d", s.mass.data(), 8, {s.nbody});
+            if (s.bits & nemo::PhaseSpaceBit) w.data("PhaseSpace", "d", s.phase.data(), 8, {s.nbody, 2, 3});
+            if (s.bits & nemo::PotentialBit) w.data("Potential", "d", s.phi.data(), 8, {s.nbody});
+            if (s.bits & nemo::AccelerationBit) w.data("Acceleration", "d", s.acc.data(), 8, {s.nbody, 3});
+            w.tes("Particles");
+            w.tes("SnapShot");
+            count++;
+        }
+        nemo::strclose(fi);
+        nemo::strclose(fo);
+        return count;
+    } catch (std::exception &) {
+        return -1;
+    }
+}
+
+// getdparam-style expression value (NEMO evaluates e.g. dtime=1/32); *ok = 0 on error
+double hc_nemo_eval(const char *expr, int *ok)
+{
+    try {
+        Expr e(expr);
+        double v = e.sum();
+        e.ws();
+        if (*e.p) throw std::runtime_error("trailing characters");
+        if (ok) *ok = 1;
+        return v;
+    } catch (std::exception &) {
+        if (ok) *ok = 0;
+        return 0.0;
+    }
+}
+
 void hc_mkplummer(int n, int seed, double *mass, double *phase) { nemo::mkplummer(n, seed, mass, phase); }
 void hc_make_testdata(int n, int seed, int cencon, double *mass, double *phase)
 {

@@ -26,7 +26,8 @@ ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "cell pool exhausted", -4: "
 EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_upload", "hc_set_box", "hc_get_box",
            "hc_build_tree", "hc_tree_summary", "hc_dump_tree", "hc_forces", "hc_forces_at", "hc_download",
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
-           "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_make_testdata"]
+           "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_make_testdata",
+           "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval"]
 
 
 class HCError(RuntimeError):
@@ -44,6 +45,17 @@ class Diag(C.Structure):
     _fields_ = [("etot", C.c_double * 3), ("keten", C.c_double * 9), ("peten", C.c_double * 9),
                 ("amten", C.c_double * 9), ("cmphase", C.c_double * 6), ("mtot", C.c_double),
                 ("n2b", C.c_int64), ("nbc", C.c_int64), ("nfcalc", C.c_int64)]
+
+
+class WalkStats(C.Structure):
+    _fields_ = [("candidates", C.c_int64), ("mixed", C.c_int64), ("entries_body", C.c_int64),
+                ("entries_cell", C.c_int64), ("borderline", C.c_int64), ("max_stack", C.c_int64),
+                ("mask_hist", C.c_int64 * 33)]
+
+    def as_dict(self):
+        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "mask_hist"}
+        d["mask_hist"] = [int(x) for x in self.mask_hist]
+        return d
 
 
 class TreeInfo(C.Structure):
@@ -78,6 +90,7 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_set_params.argtypes = [_vp, C.POINTER(Params)]
     L.hc_upload.argtypes = [_vp, _dp, _dp]
     L.hc_set_box.argtypes = [_vp, _dp, C.c_double]
+    L.hc_set_forces.argtypes = [_vp, _vp, _vp]
     L.hc_get_box.argtypes = [_vp, _dp, C.POINTER(C.c_double)]
     L.hc_build_tree.argtypes = [_vp]
     L.hc_tree_summary.argtypes = [_vp, C.POINTER(TreeInfo)]
@@ -90,6 +103,7 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_diagnostics.argtypes = [_vp, C.POINTER(Diag)]
     L.hc_direct_sample.argtypes = [_vp, _lp, C.c_int64, _dp, _dp]
     L.hc_last_timing.argtypes = [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    L.hc_walk_statistics.argtypes = [_vp, C.POINTER(WalkStats)]
     L.hc_timer_start.argtypes = [_vp]
     L.hc_timer_stop.argtypes = [_vp, C.POINTER(C.c_double)]
     L.hc_fp32_peak.argtypes = [_vp, C.POINTER(C.c_double)]
@@ -97,6 +111,9 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_mkplummer.restype = None
     L.hc_make_testdata.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
     L.hc_make_testdata.restype = None
+    L.hc_snapcopy.argtypes = [C.c_char_p, C.c_char_p]
+    L.hc_nemo_eval.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+    L.hc_nemo_eval.restype = C.c_double
     _lib = L
     return L
 
@@ -166,6 +183,11 @@ class Context:
     def download_ptr(self, phase_ptr=None, acc_ptr=None, phi_ptr=None):
         """Download to raw host pointers (any may be None)."""
         self._check(self._L.hc_download(self._h, phase_ptr, acc_ptr, phi_ptr))
+
+    def walk_stats(self) -> dict:
+        w = WalkStats()
+        self._check(self._L.hc_walk_statistics(self._h, C.byref(w)))
+        return w.as_dict()
 
     def timer_start(self):
         self._check(self._L.hc_timer_start(self._h))

@@ -1,0 +1,163 @@
+"""CPU-only checks of the library boundary and host services (no GPU calls).
+
+* the C-ABI library builds and exports every function include/hackcode_gpu.h
+  declares;
+* the host generators (mkplummer, hackcode1 nbody= data) are bit-identical to
+  the oracle and reproduce NEMO's published mkplummer fingerprint;
+* filestruct snapshots round-trip through the C++ reader/writer, including
+  byte-swapped input;
+* the drop-in programs honour NEMO's keyword rules (unknown / missing /
+  duplicated keywords, help=) without touching the GPU;
+* getdparam-style expressions evaluate as the reference's keywords do.
+"""
+import io
+import json
+import os
+import re
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from nemo_gb300 import build as B
+    B.build()
+    from nemo_gb300 import hackcode
+    return hackcode
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "hackcode_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(hc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", lib.LIBPATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\sT\s(hc_[a-z0-9_]+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    L = lib.library()
+    for n in names:
+        assert getattr(L, n) is not None
+    assert sorted(lib.EXPORTS) == sorted(names)
+
+
+def test_host_generators_match_oracle_and_pin(lib, oracle_lib):
+    O = oracle_lib
+    for n, seed in ((10240, 123), (777, 5)):
+        m1, p1 = lib.mkplummer(n, seed)
+        m2, p2 = O.mkplummer(n, seed)
+        assert np.array_equal(m1, m2) and np.array_equal(p1, p2)
+    for cencon in (False, True):
+        m1, p1 = lib.make_testdata(128, 123, cencon)
+        m2, p2 = O.make_testdata(128, 123, cencon)
+        assert np.array_equal(p1, p2) and np.array_equal(m1, m2)
+    pins = json.load(open(os.path.join(HERE, "golden", "reference_pins.json")))
+    m, ph = lib.mkplummer(10240, 123)
+    from nemo_gb300 import filestruct as fs
+    buf = io.BytesIO()
+    fs.write_snapshot(fs.Writer(buf), m, ph, 0.0)
+    path = os.path.join(HERE, "_p0.snap")
+    open(path, "wb").write(buf.getvalue())
+    try:
+        assert fs.bsf(path) == pins["nemobench_p0_bsf"]["value"]
+    finally:
+        os.remove(path)
+
+
+def _swap_file(src, dst):
+    """Rewrite a little-endian filestruct file in big-endian byte order."""
+    from nemo_gb300 import filestruct as fs
+    items = fs.read_items(src)
+    out = io.BytesIO()
+
+    def hdr(typ, tag, dims):
+        out.write(struct.pack(">h", fs.PLUR if dims else fs.SING))
+        out.write(typ.encode() + b"\0")
+        if tag is not None:
+            out.write(tag.encode() + b"\0")
+        if dims:
+            out.write(struct.pack(">%di" % (len(dims) + 1), *dims, 0))
+
+    def emit(it):
+        hdr(it.type, it.tag, it.dims)
+        if it.type == "(":
+            for s in it.items:
+                emit(s)
+            hdr(")", None, None)
+        else:
+            dt, size = fs.TYPES[it.type]
+            a = np.frombuffer(it.data, dtype=np.dtype("<" + dt) if size > 1 else dt)
+            out.write(a.astype(np.dtype(">" + dt)).tobytes() if size > 1 else a.tobytes())
+
+    for it in items:
+        emit(it)
+    open(dst, "wb").write(out.getvalue())
+
+
+def test_filestruct_roundtrip_through_cpp(lib, tmp_path):
+    from nemo_gb300 import filestruct as fs
+    rng = np.random.default_rng(3)
+    a = tmp_path / "a.snap"
+    with open(a, "wb") as f:
+        w = fs.Writer(f)
+        w.string("Headline", "round trip")
+        w.string("History", "test_host_cpu")
+        for t in (0.0, 0.5):
+            n = 37
+            fs.write_snapshot(w, rng.random(n), rng.normal(size=(n, 2, 3)), t, phi=-rng.random(n),
+                              acc=rng.normal(size=(n, 3)))
+    b = tmp_path / "b.snap"
+    assert lib.library().hc_snapcopy(str(a).encode(), str(b).encode()) == 2
+    assert open(a, "rb").read() == open(b, "rb").read()
+    # byte-swapped input is read (gethdr's swapped-magic path) and written natively
+    s = tmp_path / "s.snap"
+    _swap_file(str(a), str(s))
+    c = tmp_path / "c.snap"
+    assert lib.library().hc_snapcopy(str(s).encode(), str(c).encode()) == 2
+    assert open(a, "rb").read() == open(c, "rb").read()
+    snaps = fs.snapshots(str(c))
+    assert [x.time for x in snaps] == [0.0, 0.5] and snaps[0].phase.shape == (37, 2, 3)
+
+
+def _run(prog, *args):
+    exe = os.path.join(ROOT, "nemo_gb300", "bin", prog)
+    return subprocess.run([exe, *args], capture_output=True, text=True, timeout=60)
+
+
+def test_program_keywords(lib):
+    r = _run("hackcode1", "help=")
+    assert r.returncode == 0 and "freq" in r.stdout and "minor_freqout" in r.stdout
+    r = _run("hackcode1", "bogus=1")
+    assert r.returncode != 0 and 'Parameter "bogus" unknown' in r.stderr and "### Fatal error [hackcode1]" in r.stderr
+    r = _run("hackcode1", "tol=1", "tol=2")
+    assert r.returncode != 0 and "duplicated" in r.stderr
+    r = _run("hackforce")
+    assert r.returncode != 0 and 'Parameter "in" missing' in r.stderr
+    r = _run("hackforce", "in=/nonexistent", "out=.", "debug=1")     # system keyword accepted
+    assert r.returncode != 0 and "cannot open" in r.stderr
+
+
+@pytest.mark.parametrize("expr,val", [("1/32", 1 / 32), ("2*(3+4)", 14.0), ("-0.5", -0.5), ("2^10", 1024.0),
+                                      ("sqrt(4)+pi", 2 + np.pi), ("1e-3", 1e-3)])
+def test_keyword_expressions(lib, expr, val):
+    import ctypes as C
+    ok = C.c_int()
+    v = lib.library().hc_nemo_eval(expr.encode(), C.byref(ok))
+    assert ok.value == 1 and v == pytest.approx(val, rel=1e-15)
+
+
+def test_keyword_expression_errors(lib):
+    import ctypes as C
+    ok = C.c_int()
+    lib.library().hc_nemo_eval(b"1/", C.byref(ok))
+    assert ok.value == 0
