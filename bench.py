@@ -198,8 +198,7 @@ def run_ours(args, world, rank, local):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     def step():
-        ctx.build_tree()
-        ctx.forces()
+        ctx.evaluate()          # build + walk, replayed from a captured CUDA graph
 
     for _ in range(args.warmup):
         step()
@@ -241,8 +240,7 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         ctx.timer_start()
         ctx.upload_ptr(hm.data_ptr(), hph.data_ptr())
-        ctx.build_tree()
-        ctx.forces()
+        ctx.evaluate()
         ctx.download_ptr(None, hacc.data_ptr(), hphi.data_ptr())
         t = ctx.timer_stop()
         if i >= args.warmup:
@@ -277,8 +275,7 @@ def run_ours(args, world, rank, local):
     if args.stats:
         sctx = hc.Context(n, tol=TOL, eps=EPS, fcells=1.0, usequad=USEQUAD, count_per_body=True)
         sctx.upload(m, ph)
-        sctx.build_tree()
-        sctx.forces()
+        sctx.evaluate()
         ws["count_walk"] = sctx.walk_stats()
         sctx.close()
     clocks = clk.summary()

@@ -112,6 +112,14 @@ int hc_dump_tree(hc_ctx *ctx, int32_t *level, int32_t *corner, int32_t *count, d
  * (hc_download).  Requires hc_build_tree. */
 int hc_forces(hc_ctx *ctx);
 
+/* One full force evaluation -- hc_build_tree then hc_forces -- replayed
+ * from a CUDA graph captured on the first call (no host round trip inside). */
+int hc_evaluate(hc_ctx *ctx);
+
+/* CUDA-graph replay of hc_step / hc_evaluate on (1, default) or off (0);
+ * results are identical either way. */
+int hc_set_graphs(hc_ctx *ctx, int on);
+
 /* Forces at ntest separate test points that are not part of the tree
  * (hackforce test=, hackforce.c:206-213).  test_pos is host [ntest][3];
  * acc [ntest][3] / phi [ntest] receive the results (host). */

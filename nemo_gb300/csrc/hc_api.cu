@@ -64,7 +64,7 @@ void free_all(hc_ctx *c)
                     c->cnt_c, c->khi[0], c->khi[1], c->klo[0], c->klo[1], c->kval[0], c->kval[1], c->s_rank,
                     c->leaf_of_sorted, c->mhi, c->mlo, c->midx, c->mpos, c->dlcp, c->ccount, c->pre_info, c->pre_a,
                     c->pre_b, c->dkey[0], c->dkey[1], c->dval[0], c->dval[1], c->pre2bfs, c->parent, c->lastc,
-                    c->nodeA, c->nodeB, c->nodeQ, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->nq, c->flags,
+                    c->nodeA, c->nodeB, c->nodeQ, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->flags,
                     c->scan_tmp, c->hist, c->cand, c->ncand, c->diag_part, c->st, c->box, c->tx, c->ty, c->tz,
                     c->tax, c->tay, c->taz, c->tphi, c->tkhi[0], c->tkhi[1], c->tklo[0], c->tklo[1],
                     c->tkval[0], c->tkval[1]};
@@ -116,7 +116,6 @@ int alloc_all(hc_ctx *c)
     HC_TRY(dalloc(c, &c->ncx, mn));
     HC_TRY(dalloc(c, &c->ncy, mn));
     HC_TRY(dalloc(c, &c->ncz, mn));
-    HC_TRY(dalloc(c, &c->nq, 6 * mn));
     HC_TRY(dalloc(c, &c->flags, 4 * n + 8));
     HC_TRY(dalloc(c, &c->scan_tmp, 1024));
     const int64_t big = std::max<int64_t>(n, mn);
@@ -208,8 +207,17 @@ int staging(hc_ctx *c, Staging &s, int64_t count)
 
 }  // namespace
 
+struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    double kick = 0.0;
+    int64_t launches = 0;
+};
+
 struct hc_ctx_ext : hc_ctx {
     Staging stage;
+    GraphSlot graphs[2];          // 0: build + walk, 1: build + walk with closing kick + diagnostics
+    bool use_graphs = true;
+    double *h_diag = nullptr;     // pinned
     double *d_diag = nullptr;
     int64_t *d_idx = nullptr;
     int64_t idx_cap = 0;
@@ -247,7 +255,9 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
     b.chain_lmax = b.chain_lmin = -1;
     HC_CUDA(cudaMemcpy(c->box, &b, sizeof b, cudaMemcpyHostToDevice));
     HC_CUDA(cudaMemset(c->st, 0, 2 * sizeof(hc_status)));
-    return HC_OK;
+    HC_CUDA(cudaMallocHost((void **)&c->h_diag, 64 * sizeof(double)));
+    int r2 = hc_tree_setup(c);
+    return r2 != HC_OK ? r2 : hc_walk_setup(c);
 }
 
 void hc_destroy(hc_ctx *ctx)
@@ -259,6 +269,9 @@ void hc_destroy(hc_ctx *ctx)
     if (c->d_diag) cudaFree(c->d_diag);
     if (c->d_idx) cudaFree(c->d_idx);
     if (c->d_out) cudaFree(c->d_out);
+    if (c->h_diag) cudaFreeHost(c->h_diag);
+    for (auto &g : c->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     free_all(c);
     delete c;
 }
@@ -466,13 +479,8 @@ int hc_body_counts(hc_ctx *c, int32_t *n2b, int32_t *nbc)
     return HC_OK;
 }
 
-static int fill_diag(hc_ctx_ext *c, hc_diag *d)
+static void unpack_diag(hc_ctx_ext *c, const double *h, hc_diag *d)
 {
-    double h[36];
-    hc_diag_launch(c, c->d_diag);
-    HC_CUDA(cudaMemcpyAsync(h, c->d_diag, sizeof h, cudaMemcpyDeviceToHost, c->stream));
-    HC_CUDA(cudaStreamSynchronize(c->stream));
-    HC_CUDA(cudaGetLastError());
     std::memset(d, 0, sizeof *d);
     d->etot[1] = h[0];
     d->etot[2] = h[1];
@@ -491,7 +499,90 @@ static int fill_diag(hc_ctx_ext *c, hc_diag *d)
     d->n2b = (int64_t)c->h_st->n2b;
     d->nbc = (int64_t)c->h_st->nbc;
     d->nfcalc = c->n;
+}
+
+static int fill_diag(hc_ctx_ext *c, hc_diag *d)
+{
+    hc_diag_launch(c, c->d_diag);
+    HC_CUDA(cudaMemcpyAsync(c->h_diag, c->d_diag, 36 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    unpack_diag(c, c->h_diag, d);
     return HC_OK;
+}
+
+// One force evaluation (build + walk of every body, optional closing kick
+// and diagnostics) enqueued without host synchronisation: the body of both
+// the captured graphs and the direct path.
+static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bool with_diag)
+{
+    HC_CUDA(cudaMemsetAsync(c->st, 0, sizeof(hc_status), c->stream));
+    HC_CUDA(cudaEventRecord(c->ev[0], c->stream));
+    HC_TRY(hc_tree_build(c));
+    HC_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    HC_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    HC_TRY(hc_walk_launch(c, true, c->n, c->sidx, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
+                          nstep));
+    HC_CUDA(cudaEventRecord(c->ev[3], c->stream));
+    if (with_diag) {
+        hc_diag_launch(c, c->d_diag);
+        HC_CUDA(cudaMemcpyAsync(c->h_diag, c->d_diag, 36 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    HC_CUDA(cudaMemcpyAsync(c->h_st, c->st, sizeof(hc_status), cudaMemcpyDeviceToHost, c->stream));
+    return HC_OK;
+}
+
+static int finish_evaluation(hc_ctx_ext *c)
+{
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    int r = check_status(c);
+    if (r != HC_OK) return r;
+    cudaEventElapsedTime(&c->build_ms, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]);
+    c->have_tree = c->have_forces = true;
+    return HC_OK;
+}
+
+// Run an evaluation through a captured CUDA graph (captured on first use,
+// replayed afterwards), or directly when graphs are off.
+static int run_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nstep, bool with_diag)
+{
+    if (!c->use_graphs) {
+        c->launches = 0;
+        HC_TRY(enqueue_evaluation(c, kick_dthf, nstep, with_diag));
+        return finish_evaluation(c);
+    }
+    GraphSlot &g = c->graphs[slot];
+    if (!g.exec || g.kick != kick_dthf) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        cudaGraph_t graph = nullptr;
+        HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        c->launches = 0;
+        int r = enqueue_evaluation(c, kick_dthf, nstep, with_diag);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (r != HC_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return r;
+        }
+        if (e != cudaSuccess) {
+            c->err = std::string("stream capture: ") + cudaGetErrorString(e);
+            return HC_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            g.exec = nullptr;
+            c->err = std::string("graph instantiate: ") + cudaGetErrorString(e);
+            return HC_ERR_CUDA;
+        }
+        g.kick = kick_dthf;
+        g.launches = c->launches;
+    }
+    HC_CUDA(cudaGraphLaunch(g.exec, c->stream));
+    c->launches = g.launches;
+    return finish_evaluation(c);
 }
 
 int hc_diagnostics(hc_ctx *ctx, hc_diag *diag)
@@ -500,16 +591,35 @@ int hc_diagnostics(hc_ctx *ctx, hc_diag *diag)
     return fill_diag(static_cast<hc_ctx_ext *>(ctx), diag);
 }
 
+int hc_evaluate(hc_ctx *ctx)
+{
+    if (!ctx) return HC_ERR_ARG;
+    return run_evaluation(static_cast<hc_ctx_ext *>(ctx), 0, 0.0, 0, false);
+}
+
+int hc_set_graphs(hc_ctx *ctx, int on)
+{
+    if (!ctx) return HC_ERR_ARG;
+    static_cast<hc_ctx_ext *>(ctx)->use_graphs = on != 0;
+    return HC_OK;
+}
+
 int hc_step(hc_ctx *ctx, double dt, int64_t nstep, hc_diag *diag, double *snap_phase, double *snap_acc,
             double *snap_phi)
 {
     if (!ctx || !(dt > 0)) return HC_ERR_ARG;
     hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
-    HC_TRY(hc_build_tree(c));
-    HC_TRY(forces_self(c, 0.5 * dt, nstep));
-    if (diag) HC_TRY(fill_diag(c, diag));
+    if (nstep > 0) {
+        HC_TRY(run_evaluation(c, 1, 0.5 * dt, 1, true));   // graph: kick active
+    } else {
+        c->launches = 0;                                   // first step: no kick, not captured
+        HC_TRY(enqueue_evaluation(c, 0.0, 0, true));
+        HC_TRY(finish_evaluation(c));
+    }
+    if (diag) unpack_diag(c, c->h_diag, diag);
     if (snap_phase || snap_acc || snap_phi) HC_TRY(hc_download(c, snap_phase, snap_acc, snap_phi));
     hc_kick_drift(c, dt);
+    c->launches++;
     HC_CUDA(cudaStreamSynchronize(c->stream));
     HC_CUDA(cudaGetLastError());
     c->have_tree = false;

@@ -95,7 +95,9 @@ struct hc_ctx {
     int32_t *parent, *lastc;
     float4 *nodeA, *nodeB, *nodeQ;
     int2 *nodeC;
-    double *nm, *ncx, *ncy, *ncz, *nq;    // nq: 6 per node
+    double *nm, *ncx, *ncy, *ncz;         // FP64 mass and centre of mass per node
+    int cofm_grid;                        // co-resident blocks of the upward-pass kernel
+    int walk_blocks[4];                   // resident blocks of each walk variant
 
     // scratch
     int32_t *flags;           // n
@@ -120,9 +122,10 @@ struct hc_ctx {
 // scan / sort (hc_sort.cu)
 void hc_scan_exclusive_i32(hc_ctx *c, const int32_t *in, int32_t *out, int64_t n, int32_t *total_dev);
 int hc_radix_sort_keys(hc_ctx *c, unsigned long long *khi[2], uint32_t *klo[2], uint32_t *kval[2],
-                       int64_t n, int begin_bit, int end_bit, bool tie_fix);
+                       int64_t n, int begin_bit, int end_bit, bool tie_fix, const int *n_dev = nullptr);
 // tree (hc_tree.cu)
 int hc_tree_build(hc_ctx *c);
+int hc_tree_setup(hc_ctx *c);
 int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count, double *mass,
                       double *cm, double *quad, int32_t *bparent);
 void hc_keys_for_points(hc_ctx *c, const double *x, const double *y, const double *z, int64_t n,
@@ -131,6 +134,7 @@ void hc_keys_for_points(hc_ctx *c, const double *x, const double *y, const doubl
 int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorted,
                    const double *tx, const double *ty, const double *tz, double *oax, double *oay,
                    double *oaz, double *ophi, double kick_dthf, int64_t nstep);
+int hc_walk_setup(hc_ctx *c);
 // step (hc_step.cu)
 void hc_kick_drift(hc_ctx *c, double dt);
 void hc_diag_launch(hc_ctx *c, double *out36);

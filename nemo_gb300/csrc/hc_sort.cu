@@ -101,8 +101,10 @@ void scan_exclusive(cudaStream_t s, const T *in, T *out, int64_t n, T *part, T *
 
 // ---- radix sort passes over the 64-bit high key ----
 
-__global__ void k_radix_hist(const unsigned long long *khi, int64_t n, int shift, uint32_t *hist, int nblk)
+__global__ void k_radix_hist(const unsigned long long *khi, int64_t n, const int *n_dev, int shift, uint32_t *hist,
+                             int nblk)
 {
+    if (n_dev && *n_dev < n) n = *n_dev;
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -118,9 +120,10 @@ __global__ void k_radix_hist(const unsigned long long *khi, int64_t n, int shift
 
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(
     const unsigned long long *ihi, const uint32_t *ilo, const uint32_t *ival,
-    unsigned long long *ohi, uint32_t *olo, uint32_t *oval, int64_t n, int shift,
+    unsigned long long *ohi, uint32_t *olo, uint32_t *oval, int64_t n, const int *n_dev, int shift,
     const uint32_t *offs, int nblk)
 {
+    if (n_dev && *n_dev < n) n = *n_dev;
     __shared__ uint32_t running[256];
     __shared__ uint32_t wcnt[SORT_THREADS / 32][256];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -191,20 +194,21 @@ void hc_scan_exclusive_i32(hc_ctx *c, const int32_t *in, int32_t *out, int64_t n
 
 // Sort (khi, klo, kval)[sel] by the high key bits [begin_bit, end_bit) in
 // 8-bit passes, then order equal-high-key runs by the low key when tie_fix.
-// Returns the buffer index holding the result.
+// n bounds the launch; when n_dev is given the kernels sort min(n, *n_dev)
+// entries (a count only the device knows).  Returns the result's buffer.
 int hc_radix_sort_keys(hc_ctx *c, unsigned long long *khi[2], uint32_t *klo[2], uint32_t *kval[2],
-                       int64_t n, int begin_bit, int end_bit, bool tie_fix)
+                       int64_t n, int begin_bit, int end_bit, bool tie_fix, const int *n_dev)
 {
     int sel = 0;
     if (n <= 0) return sel;
     int nblk = (int)((n + SORT_TILE - 1) / SORT_TILE);
     int64_t nh = (int64_t)256 * nblk;
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        k_radix_hist<<<nblk, SORT_THREADS, 0, c->stream>>>(khi[sel], n, shift, c->hist, nblk);
+        k_radix_hist<<<nblk, SORT_THREADS, 0, c->stream>>>(khi[sel], n, n_dev, shift, c->hist, nblk);
         scan_exclusive<uint32_t>(c->stream, c->hist, c->hist, nh, (uint32_t *)c->scan_tmp, nullptr,
                                  &c->launches);
         k_radix_scatter<<<nblk, SORT_THREADS, 0, c->stream>>>(khi[sel], klo[sel], kval[sel], khi[sel ^ 1],
-                                                              klo[sel ^ 1], kval[sel ^ 1], n, shift,
+                                                              klo[sel ^ 1], kval[sel ^ 1], n, n_dev, shift,
                                                               c->hist, nblk);
         c->launches += 2;
         sel ^= 1;

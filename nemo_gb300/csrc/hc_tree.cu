@@ -19,10 +19,16 @@
 //      DFS pre-order directly,
 //   5. stable sort of the pre-order by depth -> breadth-first layout with the
 //      children of each cell contiguous and in subindex order 0..7,
-//   6. level-synchronous upward pass, FP64, children summed in the same order
-//      as hackcofm so mass, centre of mass and quadrupole are bit-identical.
+//   6. level-synchronous upward pass (one cooperative kernel, a grid barrier
+//      per level): mass and centre of mass in FP64, children summed in the
+//      same order as hackcofm so they are bit-identical (they decide cell
+//      openings); the quadrupole, which the walk consumes in FP32, is
+//      accumulated in FP32 from FP64 offsets.
+#include <cooperative_groups.h>
 #include <memory>
 #include "hc_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -76,7 +82,7 @@ __global__ void k_box_compact(const int32_t *outside, const int32_t *opos, int64
 // inside; each round finds the first remaining body outside, expands for
 // it, and continues after it.
 __global__ void k_box_replay(const double *px, const double *py, const double *pz, const int32_t *cand,
-                             const int32_t *ncand_p, const int32_t *mrank, hc_box *box)
+                             const int32_t *ncand_p, const int32_t *mrank, hc_box *box, hc_status *st)
 {
     __shared__ int first;
     __shared__ double rmin[3], rsize;
@@ -134,7 +140,11 @@ __global__ void k_box_replay(const double *px, const double *py, const double *p
         __syncthreads();
         pos = f + 1;
     }
-    if (threadIdx.x == 0 && doublings < 0) box->chain_lmin = -2;   // flagged below
+    if (threadIdx.x == 0 && doublings < 0) {      // non-finite position of a massive body
+        atomicCAS(&st->error, 0, HC_ERR_ARG);
+        st->info = -1;
+        return;
+    }
     if (threadIdx.x == 0) {
         box->rmin[0] = rmin[0];
         box->rmin[1] = rmin[1];
@@ -287,6 +297,8 @@ __global__ void k_post_count(int32_t *cstart, hc_box *box, int64_t maxcell, hc_s
     if (ncell > maxcell) {                      // makecell, load.c:237-239
         atomicCAS(&st->error, 0, HC_ERR_CELLS);
         st->info = (int)maxcell;
+        box->nnode = 0;                         // later kernels see an empty tree
+        box->ncell = 0;
     }
 }
 
@@ -297,7 +309,7 @@ __global__ void k_emit_preorder(const int32_t *d, const uint32_t *midx, const in
                                 unsigned long long *dkey, uint32_t *dval)
 {
     const int M = box->nmassive;
-    if (box->nnode > maxnode) return;
+    if (box->nnode > maxnode || box->nnode == 0) return;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < M; a += gridDim.x * blockDim.x) {
         int dp = a > 0 ? d[a - 1] : -1;
         int dm = dprime(d, midx, a, box);
@@ -353,6 +365,7 @@ __global__ void k_levels(const uint32_t *offs, int nblk, hc_box *box)
     int D = threadIdx.x;
     if (D <= HC_MAXLEVEL + 1) {
         int v = D <= HC_MAXLEVEL ? (int)offs[(int64_t)D * nblk] : box->nnode;
+        if (v > box->nnode) v = box->nnode;
         box->level_start[D] = v;
     }
     __syncthreads();
@@ -419,7 +432,7 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
                             const uint32_t *midx, const uint32_t *mpos, const double *mass, const double *px,
                             const double *py, const double *pz, const hc_box *box, int2 *nodeC,
                             const int32_t *lastc, float4 *nodeA, float4 *nodeB, float4 *nodeQ, double *nm,
-                            double *ncx, double *ncy, double *ncz, double *nq, int32_t *leaf_of_sorted,
+                            double *ncx, double *ncy, double *ncz, int32_t *leaf_of_sorted,
                             hc_status *st)
 {
     const int nn = box->nnode;
@@ -434,7 +447,6 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
             ncx[k] = x;
             ncy[k] = y;
             ncz[k] = z;
-            for (int q = 0; q < 6; q++) nq[(int64_t)6 * k + q] = 0.0;
             float4 A, B;
             split_hilo(x, &A.x, &B.x);
             split_hilo(y, &A.y, &B.y);
@@ -460,65 +472,81 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
     }
 }
 
-// hackcofm (load.c:183-226) for the cells of one level, children in order.
-__global__ void k_cofm_level(int D, int usequad, const hc_box *box, const int2 *nodeC, double *nm, double *ncx,
-                             double *ncy, double *ncz, double *nq, float4 *nodeA, float4 *nodeB, float4 *nodeQ)
+// hackcofm (load.c:183-226), all levels, deepest first, one grid barrier
+// per level.  Children are summed in subindex order exactly as hackcofm does.
+__global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box, const int2 *nodeC, double *nm,
+                                                  double *ncx, double *ncy, double *ncz, float4 *nodeA,
+                                                  float4 *nodeB, float4 *nodeQ)
 {
-    const int ls = box->level_start[D], le = box->level_start[D + 1];
-    const float dsqf = __double2float_rn(box->dsq[D]);
-    for (int k = ls + blockIdx.x * blockDim.x + threadIdx.x; k < le; k += gridDim.x * blockDim.x) {
-        int2 C = nodeC[k];
-        if (C.x < 0) continue;                   // body leaf
-        const int fc = C.x, nc = C.y & 255;
-        double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-        for (int i = 0; i < nc; i++) {
-            int ch = fc + i;
-            double mr = nm[ch];
-            m = dadd(m, mr);
-            cx = dadd(cx, dmul(ncx[ch], mr));
-            cy = dadd(cy, dmul(ncy[ch], mr));
-            cz = dadd(cz, dmul(ncz[ch], mr));
-        }
-        cx = ddiv(cx, m);
-        cy = ddiv(cy, m);
-        cz = ddiv(cz, m);
-        double Q[6] = {0, 0, 0, 0, 0, 0};
-        if (usequad) {
+    cg::grid_group grid = cg::this_grid();
+    const int maxd = box->nnode > 0 ? box->max_depth : -1;
+    for (int D = maxd; D >= 0; D--) {
+        const int ls = box->level_start[D], le = box->level_start[D + 1];
+        const float dsqf = __double2float_rn(box->dsq[D]);
+        for (int k = ls + (int)grid.thread_rank(); k < le; k += (int)grid.size()) {
+            const int2 C = nodeC[k];
+            if (C.x < 0) continue;                   // body leaf
+            const int fc = C.x, nc = C.y & 255;
+            double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
             for (int i = 0; i < nc; i++) {
-                int ch = fc + i;
-                double mr = nm[ch];
-                double dr[3] = {dsub(ncx[ch], cx), dsub(ncy[ch], cy), dsub(ncz[ch], cz)};
-                double drsq = dmul(dr[0], dr[0]);
-                drsq = dadd(drsq, dmul(dr[1], dr[1]));
-                drsq = dadd(drsq, dmul(dr[2], dr[2]));
-                const int jj[6] = {0, 0, 0, 1, 1, 2}, kk[6] = {0, 1, 2, 1, 2, 2};
-                bool cell = nodeC[ch].x >= 0;
-#pragma unroll
-                for (int q = 0; q < 6; q++) {
-                    double t = dmul(dmul(dr[jj[q]], dr[kk[q]]), 3.0);
-                    if (jj[q] == kk[q]) t = dsub(t, drsq);
-                    t = dmul(t, mr);
-                    if (cell) t = dadd(t, nq[(int64_t)6 * ch + q]);
-                    Q[q] = dadd(Q[q], t);
+                const int ch = fc + i;
+                const double mr = nm[ch];
+                m = dadd(m, mr);
+                cx = dadd(cx, dmul(ncx[ch], mr));
+                cy = dadd(cy, dmul(ncy[ch], mr));
+                cz = dadd(cz, dmul(ncz[ch], mr));
+            }
+            cx = ddiv(cx, m);
+            cy = ddiv(cy, m);
+            cz = ddiv(cz, m);
+            // Q = sum_child [ m (3 dr dr^T - |dr|^2 I) + Q_child ], dr = x_child - x_cm
+            float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (usequad) {
+                for (int i = 0; i < nc; i++) {
+                    const int ch = fc + i;
+                    const float mr = __double2float_rn(nm[ch]);
+                    const float dx = __double2float_rn(dsub(ncx[ch], cx)), dy = __double2float_rn(dsub(ncy[ch], cy)),
+                                dz = __double2float_rn(dsub(ncz[ch], cz));
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
+                    if (nodeC[ch].x >= 0) {
+                        q0 = nodeQ[2 * (int64_t)ch];
+                        q1 = nodeQ[2 * (int64_t)ch + 1];
+                    }
+                    Q[0] += mr * (3.f * dx * dx - r2) + q0.x;
+                    Q[1] += mr * (3.f * dx * dy) + q0.y;
+                    Q[2] += mr * (3.f * dx * dz) + q0.z;
+                    Q[3] += mr * (3.f * dy * dy - r2) + q0.w;
+                    Q[4] += mr * (3.f * dy * dz) + q1.x;
+                    Q[5] += mr * (3.f * dz * dz - r2) + q1.y;
                 }
             }
+            nm[k] = m;
+            ncx[k] = cx;
+            ncy[k] = cy;
+            ncz[k] = cz;
+            float4 A, B;
+            split_hilo(cx, &A.x, &B.x);
+            split_hilo(cy, &A.y, &B.y);
+            split_hilo(cz, &A.z, &B.z);
+            A.w = __double2float_rn(m);
+            B.w = dsqf;
+            nodeA[k] = A;
+            nodeB[k] = B;
+            nodeQ[2 * (int64_t)k] = make_float4(Q[0], Q[1], Q[2], Q[3]);
+            nodeQ[2 * (int64_t)k + 1] = make_float4(Q[4], Q[5], 0.f, 0.f);
         }
-        nm[k] = m;
-        ncx[k] = cx;
-        ncy[k] = cy;
-        ncz[k] = cz;
-        for (int q = 0; q < 6; q++) nq[(int64_t)6 * k + q] = Q[q];
-        float4 A, B;
-        split_hilo(cx, &A.x, &B.x);
-        split_hilo(cy, &A.y, &B.y);
-        split_hilo(cz, &A.z, &B.z);
-        A.w = __double2float_rn(m);
-        B.w = dsqf;
-        nodeA[k] = A;
-        nodeB[k] = B;
-        nodeQ[2 * (int64_t)k] = make_float4(__double2float_rn(Q[0]), __double2float_rn(Q[1]),
-                                            __double2float_rn(Q[2]), __double2float_rn(Q[3]));
-        nodeQ[2 * (int64_t)k + 1] = make_float4(__double2float_rn(Q[4]), __double2float_rn(Q[5]), 0.f, 0.f);
+        grid.sync();
+    }
+}
+
+// clear the child links of the nodes of this build
+__global__ void k_clear_links(const hc_box *box, int64_t maxnode, int2 *nodeC, int32_t *lastc)
+{
+    const int64_t nn = box->nnode < maxnode ? box->nnode : maxnode;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nn; k += (int64_t)gridDim.x * blockDim.x) {
+        nodeC[k] = make_int2(-1, -1);
+        lastc[k] = -1;
     }
 }
 
@@ -533,6 +561,8 @@ void hc_keys_for_points(hc_ctx *c, const double *x, const double *y, const doubl
     c->launches++;
 }
 
+// Launch the whole build on the context stream without host synchronisation
+// (graph-capturable); errors land in the device status word.
 int hc_tree_build(hc_ctx *c)
 {
     const int64_t n = c->n;
@@ -550,14 +580,8 @@ int hc_tree_build(hc_ctx *c)
     hc_scan_exclusive_i32(c, massive, mrank, n, nullptr);
     k_box_compact<<<G, B, 0, s>>>(outside, opos, n, c->cand);
     k_first_massive<<<G, B, 0, s>>>(massive, mrank, n, c->box);
-    k_box_replay<<<1, 256, 0, s>>>(c->px, c->py, c->pz, c->cand, c->ncand, mrank, c->box);
+    k_box_replay<<<1, 256, 0, s>>>(c->px, c->py, c->pz, c->cand, c->ncand, mrank, c->box, c->st);
     c->launches += 4;
-    HC_CUDA(cudaMemcpyAsync(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost, s));
-    HC_CUDA(cudaStreamSynchronize(s));
-    if (c->h_box->chain_lmin == -2) {
-        c->err = "expandbox: a massive body has a non-finite position";
-        return HC_ERR_ARG;
-    }
 
     // 2-3. keys, sort, massive compaction
     hc_keys_for_points(c, c->px, c->py, c->pz, n, c->khi[0], c->klo[0], c->kval[0]);
@@ -575,53 +599,59 @@ int hc_tree_build(hc_ctx *c)
 
     // 4. cells in pre-order
     k_lcp<<<G, B, 0, s>>>(c->mhi, c->mlo, c->midx, c->box, c->dlcp, c->st);
-    // cstart lives in flags (n+1 entries); scan over n (entries beyond M are zero)
     int32_t *cstart = c->flags + n;       // [n+1]
     HC_CUDA(cudaMemsetAsync(c->ccount, 0, sizeof(int32_t) * (n + 1), s));
     k_ccount<<<G, B, 0, s>>>(c->dlcp, c->midx, c->box, c->ccount);
     hc_scan_exclusive_i32(c, c->ccount, cstart, n + 1, nullptr);
     k_post_count<<<1, 1, 0, s>>>(cstart, c->box, c->maxcell, c->st);
-    int Gn = hc_grid(c->maxnode, B);
+    const int Gn = hc_grid(c->maxnode, B);
     k_emit_preorder<<<G, B, 0, s>>>(c->dlcp, c->midx, cstart, c->box, c->maxnode, c->pre_info, c->pre_a,
                                     c->dkey[0], c->dval[0]);
     k_cell_end<<<Gn, B, 0, s>>>(c->mhi, c->mlo, c->dlcp, c->pre_info, c->pre_a, c->box, c->maxnode, c->pre_b);
     c->launches += 6;
 
-    // Error check before the layout stage (cell overflow / coincident keys):
-    // the later kernels assume nnode <= maxnode.
-    HC_CUDA(cudaMemcpyAsync(c->h_st, c->st, sizeof(hc_status), cudaMemcpyDeviceToHost, s));
-    HC_CUDA(cudaMemcpyAsync(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost, s));
-    HC_CUDA(cudaStreamSynchronize(s));
-    if (c->h_st->error) return c->h_st->error;
-    const int nnode = c->h_box->nnode;
-    if (nnode <= 0) return HC_OK;     // no massive body: empty tree
-
-    // 5. breadth-first layout: stable sort of the pre-order by depth
+    // 5. breadth-first layout: stable sort of the pre-order by depth (count on the device)
     uint32_t *nolo[2] = {nullptr, nullptr};
-    int dsel = hc_radix_sort_keys(c, c->dkey, nolo, c->dval, nnode, 0, 8, false);
+    int dsel = hc_radix_sort_keys(c, c->dkey, nolo, c->dval, c->maxnode, 0, 8, false, &c->box->nnode);
     c->bfs2pre = c->dval[dsel];
-    {
-        int nblk = (int)((nnode + 4095) / 4096);
-        k_levels<<<1, 64, 0, s>>>(c->hist, nblk, c->box);
-    }
-    int Gm = hc_grid(nnode, B);
-    k_pre2bfs<<<Gm, B, 0, s>>>(c->bfs2pre, c->box, c->pre2bfs);
-    k_parent<<<Gm, B, 0, s>>>(c->bfs2pre, c->pre_info, c->box, c->parent);
-    HC_CUDA(cudaMemsetAsync(c->nodeC, 0xff, sizeof(int2) * nnode, s));
-    HC_CUDA(cudaMemsetAsync(c->lastc, 0xff, sizeof(int32_t) * nnode, s));
-    k_children<<<Gm, B, 0, s>>>(c->parent, c->bfs2pre, c->pre_info, c->box, c->nodeC, c->lastc);
-    k_node_init<<<Gm, B, 0, s>>>(c->bfs2pre, c->pre_info, c->pre_a, c->midx, c->mpos, c->mass, c->px, c->py,
+    k_levels<<<1, 64, 0, s>>>(c->hist, (int)((c->maxnode + 4095) / 4096), c->box);
+    k_pre2bfs<<<Gn, B, 0, s>>>(c->bfs2pre, c->box, c->pre2bfs);
+    k_parent<<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_info, c->box, c->parent);
+    k_clear_links<<<Gn, B, 0, s>>>(c->box, c->maxnode, c->nodeC, c->lastc);
+    k_children<<<Gn, B, 0, s>>>(c->parent, c->bfs2pre, c->pre_info, c->box, c->nodeC, c->lastc);
+    k_node_init<<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_info, c->pre_a, c->midx, c->mpos, c->mass, c->px, c->py,
                                  c->pz, c->box, c->nodeC, c->lastc, c->nodeA, c->nodeB, c->nodeQ, c->nm, c->ncx,
-                                 c->ncy, c->ncz, c->nq, c->leaf_of_sorted, c->st);
-    c->launches += 5;
+                                 c->ncy, c->ncz, c->leaf_of_sorted, c->st);
+    c->launches += 7;
 
-    // 6. upward pass, deepest level first
-    int Gc = hc_grid(c->maxcell > 0 ? c->maxcell : 1, B);
-    for (int D = HC_MAXLEVEL; D >= 0; D--) {
-        k_cofm_level<<<Gc, B, 0, s>>>(D, c->prm.usequad, c->box, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->nq,
-                                      c->nodeA, c->nodeB, c->nodeQ);
+    // 6. upward pass, deepest level first, one cooperative launch
+    {
+        int usequad = c->prm.usequad;
+        void *args[] = {&usequad, &c->box, &c->nodeC, &c->nm, &c->ncx, &c->ncy, &c->ncz, &c->nodeA, &c->nodeB,
+                        &c->nodeQ};
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(c->cofm_grid);
+        cfg.blockDim = dim3(256);
+        cfg.stream = s;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeCooperative;
+        attr.val.cooperative = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        HC_CUDA(cudaLaunchKernelExC(&cfg, (const void *)k_cofm_all, args));
         c->launches++;
     }
+    return HC_OK;
+}
+
+int hc_tree_setup(hc_ctx *c)
+{
+    int dev = 0, nsm = 0, per = 0;
+    HC_CUDA(cudaGetDevice(&dev));
+    HC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    HC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cofm_all, 256, 0));
+    if (per < 1) per = 1;
+    c->cofm_grid = nsm * (per > 4 ? 4 : per);
     return HC_OK;
 }
 
@@ -638,13 +668,13 @@ int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count
     auto hb = H(sizeof(uint32_t) * nn), hd = H(sizeof(int32_t) * nn), ha = H(sizeof(int32_t) * nn),
          hbb = H(sizeof(int32_t) * nn), hmhi = H(sizeof(unsigned long long) * M), hmlo = H(sizeof(uint32_t) * M),
          hmidx = H(sizeof(uint32_t) * M), hnm = H(sizeof(double) * nn), hx = H(sizeof(double) * nn),
-         hy = H(sizeof(double) * nn), hz = H(sizeof(double) * nn), hq = H(sizeof(double) * 6 * nn);
+         hy = H(sizeof(double) * nn), hz = H(sizeof(double) * nn), hq = H(sizeof(float4) * 2 * nn);
     uint32_t *bfs2pre = (uint32_t *)hb.get();
     int32_t *pd = (int32_t *)hd.get(), *pa = (int32_t *)ha.get(), *pb = (int32_t *)hbb.get();
     unsigned long long *mhi = (unsigned long long *)hmhi.get();
     uint32_t *mlo = (uint32_t *)hmlo.get(), *midx = (uint32_t *)hmidx.get();
-    double *nm = (double *)hnm.get(), *nx = (double *)hx.get(), *ny = (double *)hy.get(), *nz = (double *)hz.get(),
-           *nq = (double *)hq.get();
+    double *nm = (double *)hnm.get(), *nx = (double *)hx.get(), *ny = (double *)hy.get(), *nz = (double *)hz.get();
+    float *nq = (float *)hq.get();
     HC_CUDA(cudaMemcpy(bfs2pre, c->bfs2pre, sizeof(uint32_t) * nn, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(pd, c->pre_info, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(pa, c->pre_a, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
@@ -656,7 +686,7 @@ int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count
     HC_CUDA(cudaMemcpy(nx, c->ncx, sizeof(double) * nn, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(ny, c->ncy, sizeof(double) * nn, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(nz, c->ncz, sizeof(double) * nn, cudaMemcpyDeviceToHost));
-    HC_CUDA(cudaMemcpy(nq, c->nq, sizeof(double) * 6 * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(nq, c->nodeQ, sizeof(float4) * 2 * nn, cudaMemcpyDeviceToHost));
     auto unspread = [](unsigned long long hi, uint32_t lo, int axis) {
         // axis 0 = x (bit 2 of each digit), 1 = y, 2 = z
         unsigned v = 0;
@@ -689,7 +719,7 @@ int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count
             cm[3 * ci + 2] = nz[k];
         }
         if (quad)
-            for (int q = 0; q < 6; q++) quad[6 * ci + q] = nq[(int64_t)6 * k + q];
+            for (int q = 0; q < 6; q++) quad[6 * ci + q] = nq[(int64_t)8 * k + q];
         ci++;
     }
     return ci;

@@ -443,21 +443,25 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
 }
 
 template <bool Q, bool C>
-int launch(hc_ctx *c, WalkArgs &a)
+int configure(hc_ctx *c, int variant)
 {
     const size_t smem = sizeof(WarpSmem) * WARPS;
-    static bool configured = false;
-    if (!configured) {
-        HC_CUDA(cudaFuncSetAttribute(k_walk<Q, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    HC_CUDA(cudaFuncSetAttribute(k_walk<Q, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, nsm = 0, per_sm = 0;
     HC_CUDA(cudaGetDevice(&dev));
     HC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     HC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<Q, C>, WARPS * 32, smem));
-    if (per_sm < 1) per_sm = 1;
+    c->walk_blocks[variant] = nsm * (per_sm < 1 ? 1 : per_sm);
+    return HC_OK;
+}
+
+// No CUDA queries here: this runs inside stream capture.
+template <bool Q, bool C>
+int launch(hc_ctx *c, WalkArgs &a, int variant)
+{
+    const size_t smem = sizeof(WarpSmem) * WARPS;
     int64_t ngroups = (a.ntarget + 31) / 32;
-    int64_t blocks = (int64_t)nsm * per_sm;
+    int64_t blocks = c->walk_blocks[variant];
     int64_t need = (ngroups + WARPS - 1) / WARPS;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
@@ -506,6 +510,15 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     a.group_counter = (unsigned *)(c->st + 1);
     HC_CUDA(cudaMemsetAsync(a.group_counter, 0, sizeof(unsigned), c->stream));
     const bool count = c->prm.count_per_body && self && c->cnt_b;
-    if (c->prm.usequad) return count ? launch<true, true>(c, a) : launch<true, false>(c, a);
-    return count ? launch<false, true>(c, a) : launch<false, false>(c, a);
+    if (c->prm.usequad) return count ? launch<true, true>(c, a, 3) : launch<true, false>(c, a, 2);
+    return count ? launch<false, true>(c, a, 1) : launch<false, false>(c, a, 0);
+}
+
+int hc_walk_setup(hc_ctx *c)
+{
+    int r = configure<false, false>(c, 0);
+    if (r == HC_OK) r = configure<false, true>(c, 1);
+    if (r == HC_OK) r = configure<true, false>(c, 2);
+    if (r == HC_OK) r = configure<true, true>(c, 3);
+    return r;
 }

@@ -27,7 +27,8 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_build_tree", "hc_tree_summary", "hc_dump_tree", "hc_forces", "hc_forces_at", "hc_download",
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
            "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_make_testdata",
-           "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval"]
+           "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate",
+           "hc_set_graphs"]
 
 
 class HCError(RuntimeError):
@@ -96,6 +97,8 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_tree_summary.argtypes = [_vp, C.POINTER(TreeInfo)]
     L.hc_dump_tree.argtypes = [_vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]
     L.hc_forces.argtypes = [_vp]
+    L.hc_evaluate.argtypes = [_vp]
+    L.hc_set_graphs.argtypes = [_vp, C.c_int]
     L.hc_forces_at.argtypes = [_vp, _dp, C.c_int64, _dp, _dp]
     L.hc_download.argtypes = [_vp, _vp, _vp, _vp]
     L.hc_body_counts.argtypes = [_vp, _ip, _ip]
@@ -232,6 +235,13 @@ class Context:
 
     def forces(self):
         self._check(self._L.hc_forces(self._h))
+
+    def evaluate(self):
+        """build_tree + forces as one CUDA-graph replay."""
+        self._check(self._L.hc_evaluate(self._h))
+
+    def set_graphs(self, on: bool):
+        self._check(self._L.hc_set_graphs(self._h, int(bool(on))))
 
     def forces_at(self, test_pos):
         tp = np.ascontiguousarray(test_pos, dtype=np.float64).reshape(-1, 3)
