@@ -360,7 +360,7 @@ int hc_build_tree(hc_ctx *c)
     HC_CUDA(cudaEventRecord(c->ev[1], c->stream));
     r = check_status(c);
     if (r != HC_OK) return r;
-    cudaEventElapsedTime(&c->build_ms, c->ev[0], c->ev[1]);
+    HC_CUDA(cudaEventElapsedTime(&c->build_ms, c->ev[0], c->ev[1]));
     c->have_tree = true;
     c->have_forces = false;
     return HC_OK;
@@ -404,7 +404,7 @@ static int forces_self(hc_ctx *c, double kick_dthf, int64_t nstep)
                           nstep));
     HC_CUDA(cudaEventRecord(c->ev[3], c->stream));
     HC_TRY(check_status(c));
-    cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]);
+    HC_CUDA(cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]));
     c->have_forces = true;
     return HC_OK;
 }
@@ -439,7 +439,7 @@ int hc_forces_at(hc_ctx *ctx, const double *test_pos, int64_t ntest, double *acc
     HC_CUDA(cudaMemcpyAsync(acc, c->stage.d, sizeof(double) * 3 * ntest, cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaMemcpyAsync(phi, c->tphi, sizeof(double) * ntest, cudaMemcpyDeviceToHost, c->stream));
     HC_TRY(check_status(c));
-    cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]);
+    HC_CUDA(cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]));
     return HC_OK;
 }
 
@@ -514,16 +514,18 @@ static int fill_diag(hc_ctx_ext *c, hc_diag *d)
 // One force evaluation (build + walk of every body, optional closing kick
 // and diagnostics) enqueued without host synchronisation: the body of both
 // the captured graphs and the direct path.
-static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bool with_diag)
+static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bool with_diag, bool capturing)
 {
+    // inside stream capture an event record must be an explicit graph node
+    const unsigned rflags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     HC_CUDA(cudaMemsetAsync(c->st, 0, sizeof(hc_status), c->stream));
-    HC_CUDA(cudaEventRecord(c->ev[0], c->stream));
+    HC_CUDA(cudaEventRecordWithFlags(c->ev[0], c->stream, rflags));
     HC_TRY(hc_tree_build(c));
-    HC_CUDA(cudaEventRecord(c->ev[1], c->stream));
-    HC_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    HC_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, rflags));
+    HC_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, rflags));
     HC_TRY(hc_walk_launch(c, true, c->n, c->sidx, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
                           nstep));
-    HC_CUDA(cudaEventRecord(c->ev[3], c->stream));
+    HC_CUDA(cudaEventRecordWithFlags(c->ev[3], c->stream, rflags));
     if (with_diag) {
         hc_diag_launch(c, c->d_diag);
         HC_CUDA(cudaMemcpyAsync(c->h_diag, c->d_diag, 36 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -538,8 +540,8 @@ static int finish_evaluation(hc_ctx_ext *c)
     HC_CUDA(cudaGetLastError());
     int r = check_status(c);
     if (r != HC_OK) return r;
-    cudaEventElapsedTime(&c->build_ms, c->ev[0], c->ev[1]);
-    cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]);
+    HC_CUDA(cudaEventElapsedTime(&c->build_ms, c->ev[0], c->ev[1]));
+    HC_CUDA(cudaEventElapsedTime(&c->walk_ms, c->ev[2], c->ev[3]));
     c->have_tree = c->have_forces = true;
     return HC_OK;
 }
@@ -550,7 +552,7 @@ static int run_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nst
 {
     if (!c->use_graphs) {
         c->launches = 0;
-        HC_TRY(enqueue_evaluation(c, kick_dthf, nstep, with_diag));
+        HC_TRY(enqueue_evaluation(c, kick_dthf, nstep, with_diag, false));
         return finish_evaluation(c);
     }
     GraphSlot &g = c->graphs[slot];
@@ -560,7 +562,7 @@ static int run_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nst
         cudaGraph_t graph = nullptr;
         HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         c->launches = 0;
-        int r = enqueue_evaluation(c, kick_dthf, nstep, with_diag);
+        int r = enqueue_evaluation(c, kick_dthf, nstep, with_diag, true);
         cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
         if (r != HC_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -613,7 +615,7 @@ int hc_step(hc_ctx *ctx, double dt, int64_t nstep, hc_diag *diag, double *snap_p
         HC_TRY(run_evaluation(c, 1, 0.5 * dt, 1, true));   // graph: kick active
     } else {
         c->launches = 0;                                   // first step: no kick, not captured
-        HC_TRY(enqueue_evaluation(c, 0.0, 0, true));
+        HC_TRY(enqueue_evaluation(c, 0.0, 0, true, false));
         HC_TRY(finish_evaluation(c));
     }
     if (diag) unpack_diag(c, c->h_diag, diag);
