@@ -28,7 +28,7 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
            "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_make_testdata",
            "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate",
-           "hc_set_graphs"]
+           "hc_set_graphs", "hc_diagnostics_noalloc"]
 
 
 class HCError(RuntimeError):
@@ -98,6 +98,7 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_dump_tree.argtypes = [_vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]
     L.hc_forces.argtypes = [_vp]
     L.hc_evaluate.argtypes = [_vp]
+    L.hc_diagnostics_noalloc.argtypes = [C.c_int64] + [_vp] * 13
     L.hc_set_graphs.argtypes = [_vp, C.c_int]
     L.hc_forces_at.argtypes = [_vp, _dp, C.c_int64, _dp, _dp]
     L.hc_download.argtypes = [_vp, _vp, _vp, _vp]
