@@ -155,12 +155,75 @@ int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t nsample, double 
  * the context stream) and kernel launch count of the last call. */
 int hc_last_timing(hc_ctx *ctx, double *build_ms, double *walk_ms, int64_t *launches);
 
+/* Opening criterion of the walk.
+ * HC_CRITERION_BODY  (default): the reference's rule, per body -- open iff
+ *     tol^2 |cm - x|^2 < size^2 (subdivp, grav.c:122-131); interaction sets
+ *     identical to hackcode1's.
+ * HC_CRITERION_GROUP: one decision per 32-body group -- open iff
+ *     theta^2 dmin^2 < size^2, dmin the distance from the group's bounding box
+ *     to the cell's centre of mass (a group walk in the manner of treecode1's
+ *     walktree, treegrav.c:380-419).  No counterpart in hackcode1. */
+/* HC_CRITERION_ERROR: one decision per group -- accept iff the expansion's
+ *     leading truncation error m b^p / (dmin - b)^(p+2) is at most theta
+ *     times the group's smallest |a| from the previous force evaluation
+ *     (b: radius around the cell's centre of mass holding all its bodies;
+ *     p = 3 with quadrupoles, 2 without); the group rule at theta = 1 when
+ *     no previous accelerations exist.  No counterpart in hackcode1. */
+/* HC_CRITERION_LEARNED: the error rule decides clear cases; candidates whose
+ *     error proxy lies within a factor 8 of the budget theta * |a| are decided
+ *     by the trained network (hc_learn_*), accepted when its logit exceeds
+ *     the threshold of hc_learn_set_threshold.  No counterpart in hackcode1. */
+enum { HC_CRITERION_BODY = 0, HC_CRITERION_GROUP = 1, HC_CRITERION_ERROR = 2, HC_CRITERION_LEARNED = 3 };
+int hc_set_criterion(hc_ctx *ctx, int criterion, double theta);
+
+/* ---- learned opening criterion (no counterpart in hackcode1) ----
+ * The network: 12 features of a (group, cell) pair -> 64 -> 64 (SiLU) -> 1
+ * logit; BF16 weights, FP32 accumulation; FP32 master weights in the flat
+ * order W1[64][12], b1[64], W2[64][64], b2[64], W3[64], b3. */
+int hc_learn_nparams(void);
+int hc_learn_init(hc_ctx *ctx, uint64_t seed);
+int hc_learn_set_params(hc_ctx *ctx, const float *params, int count);
+int hc_learn_get_params(hc_ctx *ctx, float *params, int count);
+/* logits of n feature rows [n][12] (host arrays) through the walk's kernel */
+int hc_learn_infer(hc_ctx *ctx, const float *x, int64_t n, float *logits);
+/* gradient of the mean weighted binary cross-entropy over n <= 8192 rows
+ * (host arrays; w may be NULL) and the summed loss */
+int hc_learn_gradient(hc_ctx *ctx, const float *x, const float *y, const float *w, int64_t n, float *grad,
+                      float *loss);
+/* Labels from the method itself: with the tree built and accelerations of a
+ * previous evaluation on the device, walk with the error rule at budget
+ * theta, sample about `target` band candidates, and label each by comparing
+ * the cell's multipole with a refined walk of its subtree (label 1 when the
+ * group's largest relative error is at most theta).  *nsamples receives the
+ * count kept on the device. */
+int hc_learn_collect(hc_ctx *ctx, double theta, int64_t target, int64_t *nsamples);
+int hc_learn_samples(hc_ctx *ctx, float *x, float *y, float *rel, int64_t cap, int64_t *n);
+int hc_learn_load_samples(hc_ctx *ctx, const float *x, const float *y, const float *w, int64_t n);
+/* Adam on the device samples; *loss receives the last epoch's mean loss */
+int hc_learn_train(hc_ctx *ctx, int epochs, int batch, double lr, uint64_t seed, double *loss);
+int hc_learn_set_threshold(hc_ctx *ctx, double logit_threshold);
+/* label the device samples again: 1 when their measured relative error is at
+ * most rel_threshold */
+int hc_learn_relabel(hc_ctx *ctx, double rel_threshold);
+/* the band the network decides, in log2 of (error proxy / budget):
+ * [-lo, hi] (defaults 1 and 3); below it the cell is accepted, above opened */
+int hc_learn_set_band(hc_ctx *ctx, double lo, double hi);
+
+/* How the walk groups its 32 bodies per warp: HC_GROUPS_CONSECUTIVE (32
+ * bodies consecutive in key order) or HC_GROUPS_TREE (the bodies of one cell
+ * holding at most 32, siblings packed).  Results of HC_CRITERION_BODY do not
+ * depend on it; HC_CRITERION_GROUP always uses tree groups. */
+enum { HC_GROUPS_CONSECUTIVE = 0, HC_GROUPS_TREE = 1 };
+int hc_set_grouping(hc_ctx *ctx, int kind);
+
 /* Walk statistics of the last force evaluation: candidates classified,
  * candidates needing the per-body test, interaction-list entries evaluated
  * (bodies, cells; 32 lanes each), borderline decisions re-done in FP64 and the
  * deepest traversal stack. */
 typedef struct {
     int64_t candidates, mixed, entries_body, entries_cell, borderline, max_stack;
+    int64_t network;           /* candidates decided by the learned criterion's network */
+    int64_t network_rounds;    /* network evaluations (each decides up to 32 candidates) */
     int64_t mask_hist[33];   /* entries by accept-mask popcount (only with count_per_body) */
 } hc_walk_stats;
 int hc_walk_statistics(hc_ctx *ctx, hc_walk_stats *out);

@@ -11,6 +11,7 @@
 #include <memory>
 #include <vector>
 #include "hc_internal.cuh"
+#include "hc_mlp.cuh"
 
 namespace {
 
@@ -62,13 +63,18 @@ void free_all(hc_ctx *c)
 {
     void *ptrs[] = {c->mass, c->px, c->py, c->pz, c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->phi, c->cnt_b,
                     c->cnt_c, c->khi[0], c->khi[1], c->klo[0], c->klo[1], c->kval[0], c->kval[1], c->s_rank,
-                    c->leaf_of_sorted, c->mhi, c->mlo, c->midx, c->mpos, c->dlcp, c->ccount, c->pre_info, c->pre_a,
+                    c->leaf_of_sorted, c->tord, c->gstart, c->gcount, c->gcnt, c->goff, c->mhi, c->mlo, c->midx, c->mpos, c->dlcp, c->ccount, c->pre_info, c->pre_a,
                     c->pre_b, c->dkey[0], c->dkey[1], c->dval[0], c->dval[1], c->pre2bfs, c->parent, c->lastc,
                     c->nodeA, c->nodeB, c->nodeQ, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->flags,
                     c->scan_tmp, c->hist, c->cand, c->ncand, c->diag_part, c->st, c->box, c->tx, c->ty, c->tz,
                     c->tax, c->tay, c->taz, c->tphi, c->tkhi[0], c->tkhi[1], c->tklo[0], c->tklo[1],
                     c->tkval[0], c->tkval[1]};
     for (void *p : ptrs)
+        if (p) cudaFree(p);
+    void *mptrs[] = {c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_grad, c->mlp_loss, c->mlp_gpart, c->mlp_lpart,
+                     c->mlp_packed, c->sample_count, c->sample_x, c->sample_amin, c->sample_y, c->sample_rel,
+                     c->sample_w, c->sample_group, c->sample_node};
+    for (void *p : mptrs)
         if (p) cudaFree(p);
     if (c->h_st) cudaFreeHost(c->h_st);
     if (c->h_box) cudaFreeHost(c->h_box);
@@ -90,6 +96,9 @@ int alloc_all(hc_ctx *c)
         HC_TRY(dalloc(c, &c->kval[i], n));
     }
     HC_TRY(dalloc(c, &c->s_rank, n));
+    HC_TRY(dalloc(c, &c->tord, n));
+    HC_TRY(dalloc(c, &c->gstart, n));
+    HC_TRY(dalloc(c, &c->gcount, n));
     HC_TRY(dalloc(c, &c->leaf_of_sorted, n));
     HC_TRY(dalloc(c, &c->mhi, n));
     HC_TRY(dalloc(c, &c->mlo, n));
@@ -108,6 +117,8 @@ int alloc_all(hc_ctx *c)
     HC_TRY(dalloc(c, &c->pre2bfs, mn));
     HC_TRY(dalloc(c, &c->parent, mn));
     HC_TRY(dalloc(c, &c->lastc, mn));
+    HC_TRY(dalloc(c, &c->gcnt, mn + 1));
+    HC_TRY(dalloc(c, &c->goff, mn + 1));
     HC_TRY(dalloc(c, &c->nodeA, mn));
     HC_TRY(dalloc(c, &c->nodeB, mn));
     HC_TRY(dalloc(c, &c->nodeQ, 2 * mn));
@@ -124,6 +135,21 @@ int alloc_all(hc_ctx *c)
     HC_TRY(dalloc(c, &c->ncand, 4));
     HC_TRY(dalloc(c, &c->diag_part, 36 * 1024));
     HC_TRY(dalloc(c, &c->st, 2));
+    HC_TRY(dalloc(c, &c->mlp_p, hc_mlp_nparams()));
+    HC_TRY(dalloc(c, &c->mlp_m, hc_mlp_nparams()));
+    HC_TRY(dalloc(c, &c->mlp_v, hc_mlp_nparams()));
+    HC_TRY(dalloc(c, &c->mlp_grad, hc_mlp_nparams()));
+    HC_TRY(dalloc(c, &c->mlp_loss, 1));
+    c->mlp_gcap = 128;
+    HC_TRY(dalloc(c, &c->mlp_gpart, (int64_t)c->mlp_gcap * hc_mlp_nparams()));
+    HC_TRY(dalloc(c, &c->mlp_lpart, c->mlp_gcap));
+    {
+        char *pk = nullptr;
+        HC_CUDA(cudaMalloc((void **)&pk, sizeof(MlpSmem)));
+        c->mlp_packed = (MlpSmem *)pk;
+        HC_CUDA(cudaMemset(pk, 0, sizeof(MlpSmem)));
+    }
+    HC_TRY(dalloc(c, &c->sample_count, 2));
     HC_TRY(dalloc(c, &c->box, 1));
     HC_CUDA(cudaMallocHost((void **)&c->h_st, sizeof(hc_status)));
     HC_CUDA(cudaMallocHost((void **)&c->h_box, sizeof(hc_box)));
@@ -237,6 +263,8 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
     c->maxcell = (int64_t)(params->fcells * (double)nbody);   // load.c:50
     if (c->maxcell < 1) c->maxcell = 1;
     c->maxnode = nbody + c->maxcell;
+    c->mlp_band = 1.0f;
+    c->mlp_band_hi = 3.0f;
     *out = c;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         c->err = "cudaStreamCreate failed";
@@ -400,7 +428,7 @@ static int forces_self(hc_ctx *c, double kick_dthf, int64_t nstep)
     }
     reset_status(c);
     HC_CUDA(cudaEventRecord(c->ev[2], c->stream));
-    HC_TRY(hc_walk_launch(c, true, c->n, c->sidx, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
+    HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
                           nstep));
     HC_CUDA(cudaEventRecord(c->ev[3], c->stream));
     HC_TRY(check_status(c));
@@ -523,7 +551,7 @@ static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bo
     HC_TRY(hc_tree_build(c));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, rflags));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, rflags));
-    HC_TRY(hc_walk_launch(c, true, c->n, c->sidx, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
+    HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
                           nstep));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[3], c->stream, rflags));
     if (with_diag) {
@@ -656,6 +684,323 @@ int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t ns, double *acc,
     return HC_OK;
 }
 
+int hc_set_criterion(hc_ctx *ctx, int criterion, double theta)
+{
+    if (!ctx || criterion < HC_CRITERION_BODY || criterion > HC_CRITERION_LEARNED) return HC_ERR_ARG;
+    if (criterion != HC_CRITERION_BODY && !(theta >= 0.0)) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    c->criterion = criterion;
+    c->group_theta = theta;
+    for (auto &g : c->graphs)        // captured graphs bake the walk variant
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    return HC_OK;
+}
+
+int hc_set_grouping(hc_ctx *ctx, int kind)
+{
+    if (!ctx || (kind != HC_GROUPS_CONSECUTIVE && kind != HC_GROUPS_TREE)) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    c->group_kind = kind;
+    for (auto &g : c->graphs)
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    return HC_OK;
+}
+
+
+// ---------------------------------------------------------------- learned criterion
+
+static int ensure_samples(hc_ctx *c, int64_t cap)
+{
+    if (cap <= c->sample_capacity) return HC_OK;
+    void *ptrs[] = {c->sample_x, c->sample_amin, c->sample_y, c->sample_rel, c->sample_w, c->sample_group,
+                    c->sample_node};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    HC_TRY(dalloc(c, &c->sample_x, 12 * cap));
+    HC_TRY(dalloc(c, &c->sample_amin, cap));
+    HC_TRY(dalloc(c, &c->sample_y, cap));
+    HC_TRY(dalloc(c, &c->sample_rel, cap));
+    HC_TRY(dalloc(c, &c->sample_w, cap));
+    HC_TRY(dalloc(c, &c->sample_group, cap));
+    HC_TRY(dalloc(c, &c->sample_node, cap));
+    c->sample_capacity = (int)cap;
+    return HC_OK;
+}
+
+int hc_learn_nparams(void) { return hc_mlp_nparams(); }
+
+int hc_learn_set_params(hc_ctx *c, const float *p, int count)
+{
+    if (!c || !p || count != hc_mlp_nparams()) return HC_ERR_ARG;
+    HC_CUDA(cudaMemcpyAsync(c->mlp_p, p, sizeof(float) * count, cudaMemcpyHostToDevice, c->stream));
+    HC_CUDA(cudaMemsetAsync(c->mlp_m, 0, sizeof(float) * count, c->stream));
+    HC_CUDA(cudaMemsetAsync(c->mlp_v, 0, sizeof(float) * count, c->stream));
+    c->mlp_step = 0;
+    HC_TRY(hc_mlp_pack(c));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int hc_learn_get_params(hc_ctx *c, float *p, int count)
+{
+    if (!c || !p || count != hc_mlp_nparams()) return HC_ERR_ARG;
+    HC_CUDA(cudaMemcpyAsync(p, c->mlp_p, sizeof(float) * count, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    return HC_OK;
+}
+
+int hc_learn_init(hc_ctx *c, uint64_t seed)
+{
+    if (!c) return HC_ERR_ARG;
+    const int np = hc_mlp_nparams();
+    std::vector<float> p(np, 0.f);
+    uint64_t st = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto uni = [&]() {               // uniform in (-1, 1) from a 64-bit LCG
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        return ((double)(st >> 11) / (double)(1ULL << 53)) * 2.0 - 1.0;
+    };
+    const int H = 64, I = 12;
+    const double a1 = std::sqrt(6.0 / (I + H)), a2 = std::sqrt(6.0 / (H + H)), a3 = std::sqrt(6.0 / (H + 1));
+    int o = 0;
+    for (int i = 0; i < H * I; i++) p[o++] = (float)(a1 * uni());
+    o += H;
+    for (int i = 0; i < H * H; i++) p[o++] = (float)(a2 * uni());
+    o += H;
+    for (int i = 0; i < H; i++) p[o++] = (float)(a3 * uni());
+    return hc_learn_set_params(c, p.data(), np);
+}
+
+int hc_learn_infer(hc_ctx *ctx, const float *x, int64_t n, float *logits)
+{
+    if (!ctx || n < 0 || (n > 0 && (!x || !logits))) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    if (n == 0) return HC_OK;
+    HC_TRY(staging(c, c->stage, (13 * n + 1) / 2 + 1));
+    float *dx = (float *)c->stage.d, *dl = dx + 12 * n;
+    HC_CUDA(cudaMemcpyAsync(dx, x, sizeof(float) * 12 * n, cudaMemcpyHostToDevice, c->stream));
+    HC_TRY(hc_mlp_infer_impl(c, dx, n, dl));
+    HC_CUDA(cudaMemcpyAsync(logits, dl, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int hc_learn_gradient(hc_ctx *ctx, const float *x, const float *y, const float *w, int64_t n, float *grad,
+                      float *loss)
+{
+    if (!ctx || n <= 0 || !x || !y || !grad) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    if (n > (int64_t)c->mlp_gcap * 64) return HC_ERR_ARG;
+    HC_TRY(staging(c, c->stage, (14 * n + 1) / 2 + 1));
+    float *dx = (float *)c->stage.d, *dy = dx + 12 * n, *dw = dy + n;
+    HC_CUDA(cudaMemcpyAsync(dx, x, sizeof(float) * 12 * n, cudaMemcpyHostToDevice, c->stream));
+    HC_CUDA(cudaMemcpyAsync(dy, y, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+    double wsum = (double)n;
+    if (w) {
+        HC_CUDA(cudaMemcpyAsync(dw, w, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+        wsum = 0;
+        for (int64_t i = 0; i < n; i++) wsum += w[i];
+    }
+    HC_TRY(hc_mlp_grad_impl(c, dx, dy, w ? dw : nullptr, n, (float)(1.0 / wsum), c->mlp_grad, c->mlp_loss));
+    HC_CUDA(cudaMemcpyAsync(grad, c->mlp_grad, sizeof(float) * hc_mlp_nparams(), cudaMemcpyDeviceToHost,
+                            c->stream));
+    if (loss) HC_CUDA(cudaMemcpyAsync(loss, c->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int hc_learn_relabel(hc_ctx *c, double thr)
+{
+    if (!c) return HC_ERR_ARG;
+    HC_TRY(hc_relabel_impl(c, (float)thr));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    return HC_OK;
+}
+
+int hc_learn_set_band(hc_ctx *ctx, double lo, double hi)
+{
+    if (!ctx || !(lo >= 0) || !(hi >= 0)) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    c->mlp_band = (float)lo;
+    c->mlp_band_hi = (float)hi;
+    for (auto &g : c->graphs)
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    return HC_OK;
+}
+
+int hc_learn_set_threshold(hc_ctx *ctx, double t)
+{
+    if (!ctx) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    c->mlp_threshold = (float)t;
+    for (auto &g : c->graphs)
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    return HC_OK;
+}
+
+int hc_learn_collect(hc_ctx *ctx, double theta, int64_t target, int64_t *nsamples)
+{
+    if (!ctx || !(theta > 0) || target <= 0) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    HC_TRY(ensure_samples(c, target + target / 4 + 1024));
+    HC_TRY(ensure_test_capacity(c, c->n));      // label walk results go to scratch, not to the state
+    const int crit = c->criterion;
+    const double th = c->group_theta;
+    c->criterion = HC_CRITERION_LEARNED;
+    c->group_theta = theta;
+    c->collect = 1;
+    // tree of the current positions
+    HC_CUDA(cudaMemsetAsync(c->st, 0, sizeof(hc_status), c->stream));
+    int r = hc_tree_build(c);
+    if (r == HC_OK) r = check_status(c);
+    int64_t counts[2] = {0, 0};
+    for (int pass = 0; pass < 2 && r == HC_OK; pass++) {
+        // pass 0 counts the band candidates, pass 1 keeps ~target of them
+        c->collect_cap = pass == 0 ? 0 : c->sample_capacity;
+        double frac = pass == 0 ? 1.0 : std::min(1.0, (double)target / std::max<int64_t>(1, counts[0]));
+        c->keep24 = (unsigned)std::min(16777216.0, frac * 16777216.0);
+        HC_CUDA(cudaMemsetAsync(c->sample_count, 0, sizeof(int), c->stream));
+        HC_CUDA(cudaMemsetAsync(c->st, 0, sizeof(hc_status), c->stream));
+        r = hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->tax, c->tay, c->taz, c->tphi, 0.0, 0);
+        int cnt = 0;
+        if (r == HC_OK) HC_CUDA(cudaMemcpyAsync(&cnt, c->sample_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        if (r == HC_OK) r = check_status(c);
+        counts[pass] = cnt;
+    }
+    c->collect = 0;
+    c->criterion = crit;
+    c->group_theta = th;
+    if (r != HC_OK) return r;
+    const int ns = (int)std::min<int64_t>(counts[1], c->sample_capacity);
+    HC_TRY(hc_label_launch(c, ns, (float)theta));
+    std::vector<float> ones(ns > 0 ? ns : 1, 1.0f);
+    if (ns > 0) HC_CUDA(cudaMemcpyAsync(c->sample_w, ones.data(), sizeof(float) * ns, cudaMemcpyHostToDevice, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    c->nsample = ns;
+    c->band_total = counts[0];
+    if (nsamples) *nsamples = ns;
+    return HC_OK;
+}
+
+int hc_learn_samples(hc_ctx *ctx, float *x, float *y, float *rel, int64_t cap, int64_t *n)
+{
+    if (!ctx || !n) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    const int64_t k = std::min<int64_t>(cap, c->nsample);
+    if (k > 0) {
+        if (x) HC_CUDA(cudaMemcpyAsync(x, c->sample_x, sizeof(float) * 12 * k, cudaMemcpyDeviceToHost, c->stream));
+        if (y) HC_CUDA(cudaMemcpyAsync(y, c->sample_y, sizeof(float) * k, cudaMemcpyDeviceToHost, c->stream));
+        if (rel) HC_CUDA(cudaMemcpyAsync(rel, c->sample_rel, sizeof(float) * k, cudaMemcpyDeviceToHost, c->stream));
+        HC_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    *n = c->nsample;
+    return HC_OK;
+}
+
+int hc_learn_load_samples(hc_ctx *ctx, const float *x, const float *y, const float *w, int64_t n)
+{
+    if (!ctx || n <= 0 || !x || !y) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    HC_TRY(ensure_samples(c, n));
+    HC_CUDA(cudaMemcpyAsync(c->sample_x, x, sizeof(float) * 12 * n, cudaMemcpyHostToDevice, c->stream));
+    HC_CUDA(cudaMemcpyAsync(c->sample_y, y, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+    std::vector<float> ones;
+    if (!w) {
+        ones.assign(n, 1.0f);
+        w = ones.data();
+    }
+    HC_CUDA(cudaMemcpyAsync(c->sample_w, w, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    c->nsample = (int)n;
+    return HC_OK;
+}
+
+__global__ void k_gather_samples(const int *perm, int n, const float *x, const float *y, const float *w, float *ox,
+                                 float *oy, float *ow)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int j = perm[i];
+        for (int k = 0; k < 12; k++) ox[(int64_t)i * 12 + k] = x[(int64_t)j * 12 + k];
+        oy[i] = y[j];
+        ow[i] = w[j];
+    }
+}
+
+int hc_learn_train(hc_ctx *ctx, int epochs, int batch, double lr, uint64_t seed, double *loss)
+{
+    if (!ctx || epochs < 1 || batch < 64 || !(lr > 0)) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    const int n = c->nsample;
+    if (n < 64) {
+        c->err = "hc_learn_train: fewer than 64 samples";
+        return HC_ERR_STATE;
+    }
+    batch = std::min(batch, c->mlp_gcap * 64);
+    // shuffle once into the staging area (the samples are reused every epoch in this order)
+    HC_TRY(staging(c, c->stage, (int64_t)n * 8 + 8));
+    float *sx = (float *)c->stage.d, *sy = sx + 12 * (int64_t)n, *sw = sy + n;
+    int *dperm = (int *)(sw + n);
+    std::vector<int> perm(n);
+    for (int i = 0; i < n; i++) perm[i] = i;
+    uint64_t st = seed * 2862933555777941757ULL + 3037000493ULL;
+    for (int i = n - 1; i > 0; i--) {
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        const int j = (int)((st >> 33) % (uint64_t)(i + 1));
+        std::swap(perm[i], perm[j]);
+    }
+    HC_CUDA(cudaMemcpyAsync(dperm, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+    k_gather_samples<<<hc_grid(n, 256), 256, 0, c->stream>>>(dperm, n, c->sample_x, c->sample_y, c->sample_w, sx, sy, sw);
+    double last = 0;
+    std::vector<float> wv(n);
+    HC_CUDA(cudaMemcpyAsync(wv.data(), sw, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    for (int e = 0; e < epochs; e++) {
+        double esum = 0, wtot = 0;
+        for (int b0 = 0; b0 + 64 <= n; b0 += batch) {
+            const int nb = std::min(batch, n - b0);
+            double ws = 0;
+            for (int i = 0; i < nb; i++) ws += wv[b0 + i];
+            HC_TRY(hc_mlp_grad_impl(c, sx + 12 * (int64_t)b0, sy + b0, sw + b0, nb, (float)(1.0 / ws), c->mlp_grad,
+                                    c->mlp_loss));
+            c->mlp_step++;
+            HC_TRY(hc_mlp_adam_impl(c, c->mlp_grad, (float)lr, c->mlp_step));
+            float l = 0;
+            if (b0 + batch >= n - 63 || (b0 / batch) % 16 == 0) {
+                HC_CUDA(cudaMemcpyAsync(&l, c->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+                HC_CUDA(cudaStreamSynchronize(c->stream));
+                esum += l;
+                wtot += ws;
+            }
+        }
+        last = wtot > 0 ? esum / wtot : 0;
+    }
+    HC_TRY(hc_mlp_pack(c));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaGetLastError());
+    for (auto &g : c->graphs)
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    if (loss) *loss = last;
+    return HC_OK;
+}
+
 int hc_walk_statistics(hc_ctx *c, hc_walk_stats *o)
 {
     if (!c || !o) return HC_ERR_ARG;
@@ -667,6 +1012,8 @@ int hc_walk_statistics(hc_ctx *c, hc_walk_stats *o)
     o->entries_cell = (int64_t)c->h_st->nentry_c;
     o->borderline = c->h_st->nborder;
     o->max_stack = c->h_st->max_stack;
+    o->network = (int64_t)c->h_st->nmlp;
+    o->network_rounds = (int64_t)c->h_st->nmlp_rounds;
     for (int i = 0; i < 33; i++) o->mask_hist[i] = (int64_t)c->h_st->mask_hist[i];
     return HC_OK;
 }

@@ -19,6 +19,7 @@
 
 #define HC_IMAX (1 << 30)     // defs.h:124-128
 #define HC_MAXLEVEL 31        // levels 0..30
+#define HC_GROUP 32           // bodies per walk group (one warp)
 
 // Device status word (written by kernels, read by the host after a sync).
 struct hc_status {
@@ -33,6 +34,8 @@ struct hc_status {
     unsigned long long nentry_b;  // body-list entries evaluated (32 lanes each)
     unsigned long long nentry_c;  // cell-list entries evaluated
     unsigned long long mask_hist[33];  // entries by accept-mask popcount (counting walk only)
+    unsigned long long nmlp;      // learned walk: candidates decided by the network
+    unsigned long long nmlp_rounds;   // learned walk: network evaluations
 };
 
 // Root box state, kept on the device so the whole step can run without a
@@ -48,6 +51,7 @@ struct hc_box {
     int ncell;                // cells of the last build
     int max_depth;            // deepest node depth of the last build
     int nnode;                // nmassive + ncell
+    int ngroups;              // tree-aligned walk groups of the massive bodies
     int level_start[HC_MAXLEVEL + 2];  // BFS offset of each depth
     double dsq[HC_MAXLEVEL + 1];       // rsize^2 / 4^level (grav.c:86,105)
 };
@@ -75,6 +79,10 @@ struct hc_ctx {
     uint32_t *sidx;           // sorted position -> original index (all bodies)
     int32_t *s_rank;          // sorted position -> massive rank or -1
     int32_t *leaf_of_sorted;  // sorted position -> BFS node of its leaf or -1
+    uint32_t *tord;           // walk target order: massive in key order, then massless
+    int32_t *gcnt, *goff;     // groups per node, their offsets (maxnode + 1)
+    int32_t *gstart, *gcount; // tree-aligned groups: first massive rank, count
+    int group_kind;           // 0: 32 consecutive bodies, 1: tree-aligned groups
 
     // massive bodies in key order
     unsigned long long *mhi;
@@ -97,7 +105,26 @@ struct hc_ctx {
     int2 *nodeC;
     double *nm, *ncx, *ncy, *ncz;         // FP64 mass and centre of mass per node
     int cofm_grid;                        // co-resident blocks of the upward-pass kernel
-    int walk_blocks[4];                   // resident blocks of each walk variant
+    int walk_blocks[16];                  // resident blocks of each walk variant
+    // learned opening criterion: network, training state, samples
+    struct MlpSmem *mlp_packed;           // BF16 image used by the walk
+    float *mlp_p, *mlp_m, *mlp_v;         // FP32 master weights, Adam moments
+    float *mlp_gpart, *mlp_lpart, *mlp_grad, *mlp_loss;
+    int mlp_gcap;                         // blocks of one training mini-batch
+    int mlp_step;                         // Adam step count
+    float mlp_threshold;
+    float mlp_band, mlp_band_hi;          // learned walk: network band [-band, band_hi] in log2(proxy/budget)
+    int collect;                          // 1 while the label walk runs
+    unsigned keep24;
+    int collect_cap;                      // 0: count band candidates only
+    int sample_capacity;
+    int *sample_count;
+    float *sample_x, *sample_amin, *sample_y, *sample_rel, *sample_w;
+    int *sample_group, *sample_node;
+    int nsample;                          // samples held on the device
+    int64_t band_total;                   // band candidates seen by the last collection walk
+    int criterion;                        // HC_CRITERION_* of include/hackcode_gpu.h
+    double group_theta;                   // opening angle of the group criterion
 
     // scratch
     int32_t *flags;           // n
@@ -135,6 +162,16 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
                    const double *tx, const double *ty, const double *tz, double *oax, double *oay,
                    double *oaz, double *ophi, double kick_dthf, int64_t nstep);
 int hc_walk_setup(hc_ctx *c);
+struct MlpSmem;
+int hc_label_launch(hc_ctx *c, int nsample, float eps_label);
+// learned criterion network (hc_learn.cu)
+int hc_mlp_nparams();
+int hc_mlp_pack(hc_ctx *c);
+int hc_mlp_infer_impl(hc_ctx *c, const float *x_dev, int64_t n, float *logits_dev);
+int hc_mlp_grad_impl(hc_ctx *c, const float *x, const float *y, const float *w, int64_t n, float inv_norm,
+                     float *grad_dev, float *loss_dev);
+int hc_mlp_adam_impl(hc_ctx *c, const float *grad_dev, float lr, int t);
+int hc_relabel_impl(hc_ctx *c, float thr);
 // step (hc_step.cu)
 void hc_kick_drift(hc_ctx *c, double dt);
 void hc_diag_launch(hc_ctx *c, double *out36);

@@ -225,21 +225,28 @@ __global__ void k_sorted_massive(const uint32_t *sidx, const double *mass, int64
         flag[s] = mass[sidx[s]] != 0.0;
 }
 
+// Massive bodies in key order (tree input) and the walk's target order:
+// massive bodies in key order, then massless ones in key order.
 __global__ void k_mcompact(const int32_t *flag, const int32_t *rank, int64_t n, const unsigned long long *khi,
-                           const uint32_t *klo, const uint32_t *sidx, unsigned long long *mhi, uint32_t *mlo,
-                           uint32_t *midx, uint32_t *mpos, int32_t *s_rank, int32_t *leaf_of_sorted)
+                           const uint32_t *klo, const uint32_t *sidx, const hc_box *box, unsigned long long *mhi,
+                           uint32_t *mlo, uint32_t *midx, uint32_t *mpos, int32_t *s_rank, int32_t *leaf_of_sorted,
+                           uint32_t *tord)
 {
+    const int M = box->nmassive;
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
         leaf_of_sorted[s] = -1;
+        int r = rank[s];
         if (flag[s]) {
-            int r = rank[s];
             mhi[r] = khi[s];
             mlo[r] = klo[s];
             midx[r] = sidx[s];
             mpos[r] = (uint32_t)s;
             s_rank[s] = r;
-        } else
+            tord[r] = sidx[s];
+        } else {
             s_rank[s] = -1;
+            tord[M + (s - r)] = sidx[s];
+        }
     }
 }
 
@@ -457,7 +464,7 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
             nodeB[k] = B;
             nodeQ[2 * (int64_t)k] = make_float4(0.f, 0.f, 0.f, 0.f);
             nodeQ[2 * (int64_t)k + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-            nodeC[k] = make_int2(-1 - (int)s, D << 8);
+            nodeC[k] = make_int2(-1 - a, D << 8);      // body leaf: -1 - massive rank
             leaf_of_sorted[s] = k;
         } else {
             int fc = nodeC[k].x, nc = lastc[k] - fc + 1;
@@ -499,6 +506,16 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             cx = ddiv(cx, m);
             cy = ddiv(cy, m);
             cz = ddiv(cz, m);
+            // bmax: radius around the centre of mass holding every body of the
+            // cell (children's extents shifted to the new centre)
+            float bmax = 0.f;
+            for (int i = 0; i < nc; i++) {
+                const int ch = fc + i;
+                const float dx = __double2float_rn(dsub(ncx[ch], cx)), dy = __double2float_rn(dsub(ncy[ch], cy)),
+                            dz = __double2float_rn(dsub(ncz[ch], cz));
+                const float bc = nodeC[ch].x >= 0 ? nodeQ[2 * (int64_t)ch + 1].w : 0.f;
+                bmax = fmaxf(bmax, sqrtf(dx * dx + dy * dy + dz * dz) + bc);
+            }
             // Q = sum_child [ m (3 dr dr^T - |dr|^2 I) + Q_child ], dr = x_child - x_cm
             float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (usequad) {
@@ -534,7 +551,7 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             nodeA[k] = A;
             nodeB[k] = B;
             nodeQ[2 * (int64_t)k] = make_float4(Q[0], Q[1], Q[2], Q[3]);
-            nodeQ[2 * (int64_t)k + 1] = make_float4(Q[4], Q[5], 0.f, 0.f);
+            nodeQ[2 * (int64_t)k + 1] = make_float4(Q[4], Q[5], 0.f, bmax);
         }
         grid.sync();
     }
@@ -551,6 +568,82 @@ __global__ void k_clear_links(const hc_box *box, int64_t maxnode, int2 *nodeC, i
 }
 
 __global__ void k_set_nmassive(const int32_t *total, hc_box *box) { box->nmassive = *total; }
+
+// ---------------- walk groups aligned with the tree ----------------
+// A group is a run of massive bodies (in key order) that lie in one cell of
+// at most HC_GROUP bodies: the cells (and lone bodies) with <= HC_GROUP bodies
+// whose parent has more, consecutive siblings packed while they fit.
+
+__device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t *pre_a, const int32_t *pre_b, int k,
+                                          int *first)
+{
+    const uint32_t p = bfs2pre[k];
+    const int a = pre_a[p];
+    if (a < 0) {
+        *first = -1 - a;
+        return 1;
+    }
+    *first = a;
+    return pre_b[p] - a + 1;
+}
+
+template <bool EMIT>
+__global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const int32_t *pre_b, const int32_t *parent,
+                         const int2 *nodeC, const hc_box *box, int64_t maxnode, int32_t *ng, const int32_t *goff,
+                         int32_t *gstart, int32_t *gcount)
+{
+    const int nn = box->nnode;
+    for (int64_t kk = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; kk < maxnode;
+         kk += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)kk;
+        if (k >= nn) {
+            if (!EMIT) ng[k] = 0;
+            continue;
+        }
+        int first;
+        const int cnt = node_count(bfs2pre, pre_a, pre_b, k, &first);
+        int out = EMIT ? goff[k] : 0, packs = 0;
+        if (cnt <= HC_GROUP) {                     // only the root can be a small group on its own here
+            if (parent[k] < 0) {
+                if (EMIT) {
+                    gstart[out] = first;
+                    gcount[out] = cnt;
+                }
+                packs = 1;
+            }
+        } else {
+            const int fc = nodeC[k].x, nc = nodeC[k].y & 255;
+            int cur = 0, cur_first = 0;
+            for (int i = 0; i < nc; i++) {
+                int f;
+                const int cc = node_count(bfs2pre, pre_a, pre_b, fc + i, &f);
+                if (cc > HC_GROUP || cur + cc > HC_GROUP) {
+                    if (cur > 0) {
+                        if (EMIT) {
+                            gstart[out + packs] = cur_first;
+                            gcount[out + packs] = cur;
+                        }
+                        packs++;
+                        cur = 0;
+                    }
+                    if (cc > HC_GROUP) continue;
+                }
+                if (cur == 0) cur_first = f;
+                cur += cc;
+            }
+            if (cur > 0) {
+                if (EMIT) {
+                    gstart[out + packs] = cur_first;
+                    gcount[out + packs] = cur;
+                }
+                packs++;
+            }
+        }
+        if (!EMIT) ng[k] = packs;
+    }
+}
+
+__global__ void k_set_ngroups(const int32_t *goff, int64_t maxnode, hc_box *box) { box->ngroups = goff[maxnode]; }
 
 }  // namespace
 
@@ -593,8 +686,8 @@ int hc_tree_build(hc_ctx *c)
     k_sorted_massive<<<G, B, 0, s>>>(c->sidx, c->mass, n, sflag);
     hc_scan_exclusive_i32(c, sflag, srank, n, c->flags + 2 * n);
     k_set_nmassive<<<1, 1, 0, s>>>(c->flags + 2 * n, c->box);
-    k_mcompact<<<G, B, 0, s>>>(sflag, srank, n, c->khi[sel], c->klo[sel], c->sidx, c->mhi, c->mlo, c->midx,
-                               c->mpos, c->s_rank, c->leaf_of_sorted);
+    k_mcompact<<<G, B, 0, s>>>(sflag, srank, n, c->khi[sel], c->klo[sel], c->sidx, c->box, c->mhi, c->mlo,
+                               c->midx, c->mpos, c->s_rank, c->leaf_of_sorted, c->tord);
     c->launches += 3;
 
     // 4. cells in pre-order
@@ -641,6 +734,15 @@ int hc_tree_build(hc_ctx *c)
         HC_CUDA(cudaLaunchKernelExC(&cfg, (const void *)k_cofm_all, args));
         c->launches++;
     }
+
+    // 7. walk groups aligned with the tree
+    k_groups<false><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->pre_b, c->parent, c->nodeC,
+                                     c->box, c->maxnode, c->gcnt, nullptr, nullptr, nullptr);
+    hc_scan_exclusive_i32(c, c->gcnt, c->goff, c->maxnode + 1, nullptr);
+    k_set_ngroups<<<1, 1, 0, s>>>(c->goff, c->maxnode, c->box);
+    k_groups<true><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->pre_b, c->parent, c->nodeC, c->box, c->maxnode,
+                                    nullptr, c->goff, c->gstart, c->gcount);
+    c->launches += 3;
     return HC_OK;
 }
 

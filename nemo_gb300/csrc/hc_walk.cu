@@ -32,7 +32,9 @@
 //
 // Flop count per interaction (FMA = 2, rsqrt = 1): monopole 20, quadrupole
 // cell 59.  These are the per-interaction figures used for the roofline.
+#include <cstring>
 #include "hc_internal.cuh"
+#include "hc_mlp.cuh"
 
 namespace {
 
@@ -41,6 +43,17 @@ constexpr int STACK = 256;      // traversal stack entries per warp (deepest see
 constexpr int BCAP = 64;        // body interaction list entries per warp
 constexpr int CCAP = 64;        // cell interaction list entries per warp
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int QCAP = 64;        // learned walk: queued band candidates per warp
+
+// Learned walk, per warp: band candidates waiting for the network (the
+// scalars their features need) and the feature tile of one network round.
+struct QueueSmem {
+    __nv_bfloat16 x[32 * MLP_XS];     // features of the round's rows
+    int node[QCAP];
+    unsigned mask[QCAP];
+    float dmin2[QCAP], dmax2[QCAP], p[QCAP];
+    float z[32];                      // the round's logits
+};
 
 struct WarpSmem {
     uint2 stack[STACK];         // x = first node << 3 | (count - 1), y = lane mask
@@ -69,7 +82,68 @@ struct WalkArgs {
     double *vx, *vy, *vz;
     hc_status *st;
     unsigned *group_counter;
+    const int32_t *gstart, *gcount;       // tree-aligned groups of the massive targets
+    int use_table;                        // 1: table groups, then massless targets in 32s
+    float eps_acc;                        // MODE 2/3 error budget relative to |a|
+    const double *pax, *pay, *paz;        // MODE 2/3: accelerations of the previous evaluation
+    const MlpSmem *mlp;                   // MODE 3: packed network
+    float mlp_threshold;                  // MODE 3: accept iff logit > threshold
+    float band;                           // MODE 3: network band in log2(proxy / budget): [-band, band_hi]
+    float band_hi;
+    int collect;                          // MODE 3: decide analytically, record sampled band candidates
+    unsigned keep24;                      // sampling threshold on a 24-bit hash
+    int sample_cap;
+    int *sample_count;
+    float *sample_x;                      // [cap][12]
+    int *sample_group, *sample_node;
+    float *sample_amin;
 };
+
+// Features of a (group, cell) pair for the opening network; logarithms are
+// base 2 and scaled to O(1).  p is log2(error proxy / (eps amin)).
+__device__ __forceinline__ void cell_features_inl(float *f, float dmin2, float dmax2, float dsq, float m, float b, float gap,
+                                              float4 Q0, float4 Q1, float amin, float rg2, float eps2, int depth,
+                                              int ngroup, float p_raw)
+{
+    const float L_dmin = 0.5f * __log2f(fmaxf(dmin2, 1e-30f));
+    const float qf = sqrtf(Q0.x * Q0.x + Q0.w * Q0.w + Q1.y * Q1.y +
+                           2.f * (Q0.y * Q0.y + Q0.z * Q0.z + Q1.x * Q1.x));
+    f[0] = 0.5f * __log2f(fmaxf(dsq, 1e-30f)) - L_dmin;                 // size / dmin
+    f[1] = __log2f(fmaxf(b, 1e-30f)) - L_dmin;                           // bmax / dmin
+    f[2] = __log2f(fmaxf(m, 1e-30f)) - 2.f * L_dmin - __log2f(fmaxf(amin, 1e-30f));
+    f[3] = p_raw;                                                        // truncation-error proxy
+    f[4] = __log2f(fmaxf(qf, 1e-30f)) - __log2f(fmaxf(m * b * b, 1e-30f));
+    f[5] = 0.5f * __log2f(fmaxf(rg2, 1e-30f)) - L_dmin;                  // group extent / dmin
+    f[6] = L_dmin - 0.5f * __log2f(fmaxf(dmax2, 1e-30f));                // dmin / dmax
+    f[7] = __log2f(fmaxf(Q1.z, 1.f));                                    // bodies in the cell
+    f[8] = 0.5f * __log2f(fmaxf(eps2, 1e-30f)) - L_dmin;                 // softening / dmin
+    f[9] = (float)depth;
+    f[10] = (float)ngroup;
+    f[11] = __log2f(fmaxf(gap, 1e-30f)) - L_dmin;
+    const float scale[12] = {0.5f, 0.25f, 0.125f, 0.25f, 0.25f, 0.25f, 0.5f, 0.125f, 0.125f, 0.0625f, 0.03125f, 0.5f};
+#pragma unroll
+    for (int i = 0; i < 12; i++) f[i] = fminf(8.f, fmaxf(-8.f, f[i] * scale[i]));
+}
+
+
+// Out-of-line copy for the sampling path (label collection), which is rare.
+__device__ __noinline__ void cell_features(float *f, float dmin2, float dmax2, float dsq, float m, float b, float gap,
+                                           float4 Q0, float4 Q1, float amin, float rg2, float eps2, int depth,
+                                           int ngroup, float p_raw)
+{
+    cell_features_inl(f, dmin2, dmax2, dsq, m, b, gap, Q0, Q1, amin, rg2, eps2, depth, ngroup, p_raw);
+}
+
+__device__ __forceinline__ unsigned hash2(unsigned a, unsigned b)
+{
+    unsigned h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u + (a << 6) + (a >> 2));
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
 
 __device__ __forceinline__ float wmin(float v)
 {
@@ -155,17 +229,30 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
     }
 }
 
-template <bool QUAD, bool COUNT>
-__global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
+// MODE 0: the reference's per-body opening rule (exact interaction sets).
+// MODE 1: group rule -- a cell is accepted for the whole group when
+//         tol^2 * dmin^2 >= size^2 with dmin the distance from the group's
+//         bounding box to the cell's centre of mass, else opened for all.
+// MODE 2: group error rule -- accepted when the leading truncation error of
+//         its expansion, m b^p / (dmin - b)^(p+2) (b: radius holding the
+//         cell's bodies; p = 3 with quadrupoles, 2 without), is at most
+//         eps_acc times the group's smallest |a| of the previous evaluation.
+template <bool QUAD, bool COUNT, int MODE>
+__global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs g)
 {
     extern __shared__ float4 smem_raw[];
     WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[threadIdx.x >> 5];
+    // MODE 3: per-warp queues after the warp areas; the network's weights are
+    // read through L1 from global memory (small, shared by every warp)
+    QueueSmem *Qs = reinterpret_cast<QueueSmem *>(reinterpret_cast<WarpSmem *>(smem_raw) + WARPS) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    const int64_t ngroups = (g.ntarget + 31) / 32;
+    const int64_t nmassive = g.use_table ? g.box->nmassive : 0;
+    const int64_t ng_table = g.use_table ? g.box->ngroups : 0;
+    const int64_t ngroups = ng_table + (g.ntarget - nmassive + 31) / 32;
     const int nnode = g.box->nnode;
     const float tol2 = g.tol2f, eps2 = g.eps2f;
-    unsigned long long tot_b = 0, tot_c = 0, st_cand = 0, st_mixed = 0, st_eb = 0, st_ec = 0;
+    unsigned long long tot_b = 0, tot_c = 0, st_cand = 0, st_mixed = 0, st_eb = 0, st_ec = 0, st_mlp = 0, st_rounds = 0;
     int max_sp = 0, nborder = 0;
 
     while (true) {
@@ -176,9 +263,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
             grp = (int64_t)__shfl_sync(FULL, v, 0);
         }
         if (grp >= ngroups) break;
-        const int64_t s0 = grp * 32;
+        int64_t s0, cnt;
+        if (grp < ng_table) {
+            s0 = g.gstart[grp];
+            cnt = g.gcount[grp];
+        } else {
+            s0 = nmassive + (grp - ng_table) * 32;
+            cnt = g.ntarget - s0 < 32 ? g.ntarget - s0 : 32;
+        }
         const int64_t s = s0 + lane;
-        const bool valid = s < g.ntarget;
+        const bool valid = lane < cnt;
         const unsigned vmask = __ballot_sync(FULL, valid);
         const uint32_t o = g.tsorted[valid ? s : s0];
         const double xd = g.tx[o], yd = g.ty[o], zd = g.tz[o];
@@ -202,6 +296,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
         const float gminx = wmin(bx), gmaxx = wmax(bx), gminy = wmin(by), gmaxy = wmax(by), gminz = wmin(bz),
                     gmaxz = wmax(bz);
         const float rg2 = wmax(bx * bx + by * by + bz * bz);
+        float amin = 0.f;                        // MODE 2: group's smallest |a| (previous evaluation)
+        if (MODE >= 2) {
+            const double axo = g.pax[o], ayo = g.pay[o], azo = g.paz[o];
+            amin = wmin(valid ? __double2float_rn(sqrt(axo * axo + ayo * ayo + azo * azo)) : 3.0e38f);
+        }
         const float cR = 2e-6f * tol2 * rg2;     // absolute band term of the FP32 decision
 
         float sphi = 0.f, sax = 0.f, say = 0.f, saz = 0.f;   // Kahan sums
@@ -256,22 +355,49 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
             sp = 1;
         }
         __syncwarp();
-        while (sp > 0) {
-            // ---- gather up to 32 candidates from the top of the stack ----
+        int qn = 0;                                          // MODE 3: queued band candidates
+        while (sp > 0 || qn > 0) {
             int ncand = 0, my_node = 0;
             unsigned my_mask = 0;
-            while (ncand < 32 && sp > 0) {
+            // MODE 3: a network round decides the first (up to) 32 queued candidates
+            const bool mlp_round = MODE == 3 && (qn >= 32 || sp == 0);
+            float logit = 0.f, q_dmin2 = 0.f, q_dmax2 = 0.f, q_p = 0.f;
+            if (mlp_round) {
+                ncand = qn < 32 ? qn : 32;
+                if (lane < ncand) {
+                    my_node = Qs->node[lane];
+                    my_mask = Qs->mask[lane];
+                    q_dmin2 = Qs->dmin2[lane];
+                    q_dmax2 = Qs->dmax2[lane];
+                    q_p = Qs->p[lane];
+                }
+                __syncwarp();
+                // shift the rest of the queue down
+                const int rest = qn - ncand;
+                if (lane < rest) {
+                    Qs->node[lane] = Qs->node[32 + lane];
+                    Qs->mask[lane] = Qs->mask[32 + lane];
+                    Qs->dmin2[lane] = Qs->dmin2[32 + lane];
+                    Qs->dmax2[lane] = Qs->dmax2[32 + lane];
+                    Qs->p[lane] = Qs->p[32 + lane];
+                }
+                qn = rest;
+                st_mlp += ncand;
+                st_rounds++;
+            }
+            // ---- gather up to 32 candidates from the top of the stack ----
+            while (!mlp_round && ncand < 32 && sp > 0) {
                 const uint2 e = S.stack[sp - 1];
-                const int start = (int)(e.x >> 3), cnt = (int)(e.x & 7u) + 1;
-                const int take = min(cnt, 32 - ncand);
+                const int start = (int)(e.x >> 3), ecnt = (int)(e.x & 7u) + 1;
+                const int take = min(ecnt, 32 - ncand);
                 const int rel = lane - ncand;
                 if (rel >= 0 && rel < take) {
-                    my_node = start + cnt - take + rel;
+                    my_node = start + ecnt - take + rel;
                     my_mask = e.y;
                 }
                 ncand += take;
-                if (take == cnt) sp--;
-                else if (lane == 0) S.stack[sp - 1].x = ((unsigned)start << 3) | (unsigned)(cnt - take - 1);
+                if (take == ecnt) sp--;
+                else if (lane == 0) S.stack[sp - 1].x = ((unsigned)start << 3) | (unsigned)(ecnt - take - 1);
             }
             __syncwarp();
             const bool have = lane < ncand && my_node < nnode;
@@ -285,13 +411,35 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
                 B = g.nodeB[my_node];
                 C = g.nodeC[my_node];
             }
+            if (MODE == 3 && mlp_round) {
+                // lane r builds the feature row of the round's candidate r (rows
+                // beyond the round are zero); then the warp evaluates the network
+                uint32_t *row = reinterpret_cast<uint32_t *>(Qs->x) + lane * (MLP_XS / 2);
+                uint32_t w[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+                if (have) {
+                    const float4 Q0 = g.nodeQ[2 * (int64_t)my_node], Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
+                    float f[12];
+                    cell_features_inl(f, q_dmin2, q_dmax2, B.w, A.w, Q1.w, sqrtf(q_dmin2) - Q1.w, Q0, Q1, amin, rg2,
+                                      eps2, C.y >> 8, (int)cnt, q_p);
+#pragma unroll
+                    for (int k = 0; k < 6; k++) w[k] = pack_bf16(f[2 * k], f[2 * k + 1]);
+                }
+#pragma unroll
+                for (int k = 0; k < 6; k++) row[k] = w[k];
+#pragma unroll
+                for (int k = 6; k < MLP_XS / 2; k++) row[k] = 0u;
+                __syncwarp();
+                logit = mlp_warp_lean(*g.mlp, Qs->x, Qs->z, ncand);
+            }
             const float cx = (A.x - ghx) + (B.x - glx), cy = (A.y - ghy) + (B.y - gly), cz = (A.z - ghz) + (B.z - glz);
             const bool isbody = C.x < 0;
             unsigned openm = 0, accm = 0;
             bool mixed = false;
+            bool band = false;                 // MODE 3: queued for the network
+            float bd_dmin2 = 0.f, bd_dmax2 = 0.f, bd_p = 0.f;
             if (have) {
                 if (isbody) {
-                    const int64_t slot = (int64_t)(-1 - C.x) - s0;
+                    const int64_t slot = (int64_t)(-1 - C.x) - s0;     // leaf holds its massive rank
                     const unsigned self = (g.self_mode && slot >= 0 && slot < 32) ? (1u << slot) : 0u;
                     accm = my_mask & ~self;
                 } else {
@@ -305,12 +453,77 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
                     const float dmin2 = ex * ex + ey * ey + ez * ez;
                     const float dmax2 = fx * fx + fy * fy + fz * fz;
                     const float tmin = tol2 * dmin2, tmax = tol2 * dmax2;
-                    if (tmin - dsq > 8e-6f * tmin + cR) accm = my_mask;          // every body accepts
+                    if (MODE == 3 && mlp_round) {
+                        if (logit > g.mlp_threshold) accm = my_mask;
+                        else openm = my_mask;
+                    } else if (MODE == 1 || (MODE >= 2 && !(amin > 0.f))) {
+                        if (tmin >= dsq) accm = my_mask;
+                        else openm = my_mask;
+                    } else if (MODE == 3) {
+                        const float4 Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
+                        const float b = Q1.w;
+                        const float dmin = sqrtf(dmin2), gap = dmin - b;
+                        float p_raw = 1e30f;
+                        if (gap > 0.f && tmin >= dsq * 0.0625f) {
+                            const float gi = 1.f / gap, bg = b * gi;
+                            const float err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
+                            p_raw = __log2f(fmaxf(err, 1e-38f)) - __log2f(g.eps_acc * amin);
+                        }
+                        if (p_raw < -g.band) accm = my_mask;
+                        else if (p_raw > g.band_hi) openm = my_mask;
+                        else if (g.collect) {
+                            // label walk: analytic decision, sampled record of the band candidate
+                            if (p_raw <= 0.f) accm = my_mask;
+                            else openm = my_mask;
+                            if ((hash2((unsigned)grp, (unsigned)my_node) >> 8) < g.keep24) {
+                                const int slot = atomicAdd(g.sample_count, 1);
+                                if (slot < g.sample_cap) {
+                                    float f[12];
+                                    cell_features(f, dmin2, dmax2, dsq, A.w, b, gap, g.nodeQ[2 * (int64_t)my_node], Q1,
+                                                  amin, rg2, eps2, C.y >> 8, (int)cnt, p_raw);
+                                    for (int k = 0; k < 12; k++) g.sample_x[(int64_t)slot * 12 + k] = f[k];
+                                    g.sample_group[slot] = (int)grp;
+                                    g.sample_node[slot] = my_node;
+                                    g.sample_amin[slot] = amin;
+                                }
+                            }
+                        } else {
+                            // queue for the network: decision in a later round
+                            band = true;
+                            bd_dmin2 = dmin2;
+                            bd_dmax2 = dmax2;
+                            bd_p = p_raw;
+                        }
+                    } else if (MODE == 2) {
+                        const float b = g.nodeQ[2 * (int64_t)my_node + 1].w;
+                        const float gap = sqrtf(dmin2) - b;
+                        bool acc_ok = gap > 0.f && tmin >= dsq * 0.0625f;     // never beyond size/dmin = 4
+                        if (acc_ok) {
+                            const float gi = 1.f / gap, bg = b * gi;
+                            const float err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
+                            acc_ok = err <= g.eps_acc * amin;
+                        }
+                        if (acc_ok) accm = my_mask;
+                        else openm = my_mask;
+                    } else if (tmin - dsq > 8e-6f * tmin + cR) accm = my_mask;  // every body accepts
                     else if (dsq - tmax > 8e-6f * tmax + cR) openm = my_mask;    // every body opens
                     else mixed = true;
                 }
             }
-            unsigned mixedb = __ballot_sync(FULL, mixed);
+            if (MODE == 3) {                   // enqueue band candidates
+                const unsigned qb = __ballot_sync(FULL, band);
+                if (band) {
+                    const int row = qn + __popc(qb & lt);
+                    Qs->node[row] = my_node;
+                    Qs->mask[row] = my_mask;
+                    Qs->dmin2[row] = bd_dmin2;
+                    Qs->dmax2[row] = bd_dmax2;
+                    Qs->p[row] = bd_p;
+                }
+                qn += __popc(qb);
+                __syncwarp();
+            }
+            unsigned mixedb = MODE == 0 ? __ballot_sync(FULL, mixed) : 0u;
             st_cand += ncand;
             st_mixed += __popc(mixedb);
             while (mixedb) {
@@ -439,33 +652,38 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk(WalkArgs g)
         atomicAdd(&g.st->nmixed, st_mixed);
         atomicAdd(&g.st->nentry_b, st_eb);
         atomicAdd(&g.st->nentry_c, st_ec);
+        if (MODE == 3) {
+            atomicAdd(&g.st->nmlp, st_mlp);
+            atomicAdd(&g.st->nmlp_rounds, st_rounds);
+        }
     }
 }
 
-template <bool Q, bool C>
+constexpr size_t walk_smem(int mode) { return sizeof(WarpSmem) * WARPS + (mode == 3 ? sizeof(QueueSmem) * WARPS : 0); }
+
+template <bool Q, bool C, int M>
 int configure(hc_ctx *c, int variant)
 {
-    const size_t smem = sizeof(WarpSmem) * WARPS;
-    HC_CUDA(cudaFuncSetAttribute(k_walk<Q, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = walk_smem(M);
+    HC_CUDA(cudaFuncSetAttribute(k_walk<Q, C, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, nsm = 0, per_sm = 0;
     HC_CUDA(cudaGetDevice(&dev));
     HC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    HC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<Q, C>, WARPS * 32, smem));
+    HC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<Q, C, M>, WARPS * 32, smem));
     c->walk_blocks[variant] = nsm * (per_sm < 1 ? 1 : per_sm);
     return HC_OK;
 }
 
 // No CUDA queries here: this runs inside stream capture.
-template <bool Q, bool C>
+template <bool Q, bool C, int M>
 int launch(hc_ctx *c, WalkArgs &a, int variant)
 {
-    const size_t smem = sizeof(WarpSmem) * WARPS;
-    int64_t ngroups = (a.ntarget + 31) / 32;
-    int64_t blocks = c->walk_blocks[variant];
-    int64_t need = (ngroups + WARPS - 1) / WARPS;
-    if (blocks > need) blocks = need;
+    const size_t smem = walk_smem(M);
+    int64_t blocks = c->walk_blocks[variant];               // persistent: groups are fetched dynamically
+    int64_t need = ((a.ntarget + 31) / 32 + WARPS - 1) / WARPS;
+    if (!a.use_table && blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
-    k_walk<Q, C><<<(unsigned)blocks, WARPS * 32, smem, c->stream>>>(a);
+    k_walk<Q, C, M><<<(unsigned)blocks, WARPS * 32, smem, c->stream>>>(a);
     c->launches++;
     return HC_OK;
 }
@@ -508,17 +726,206 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     a.vz = c->vz;
     a.st = c->st;
     a.group_counter = (unsigned *)(c->st + 1);
+    a.pax = c->ax;
+    a.pay = c->ay;
+    a.paz = c->az;
+    a.gstart = c->gstart;
+    a.gcount = c->gcount;
+    a.use_table = (self && (c->group_kind == 1 || c->criterion != HC_CRITERION_BODY)) ? 1 : 0;
     HC_CUDA(cudaMemsetAsync(a.group_counter, 0, sizeof(unsigned), c->stream));
     const bool count = c->prm.count_per_body && self && c->cnt_b;
-    if (c->prm.usequad) return count ? launch<true, true>(c, a, 3) : launch<true, false>(c, a, 2);
-    return count ? launch<false, true>(c, a, 1) : launch<false, false>(c, a, 0);
+    const int v = (c->prm.usequad ? 2 : 0) + (count ? 1 : 0);
+    a.eps_acc = (float)c->group_theta;
+    if (c->criterion == HC_CRITERION_GROUP) {
+        a.tol2d = c->group_theta * c->group_theta;
+        a.tol2f = (float)a.tol2d;
+        switch (v) {
+        case 0: return launch<false, false, 1>(c, a, 4);
+        case 1: return launch<false, true, 1>(c, a, 5);
+        case 2: return launch<true, false, 1>(c, a, 6);
+        default: return launch<true, true, 1>(c, a, 7);
+        }
+    }
+    if (c->criterion == HC_CRITERION_LEARNED) {
+        a.tol2d = 0.25;     // fallback geometric rule (no previous accelerations): theta = 0.5
+        a.tol2f = 0.25f;
+        a.mlp = c->mlp_packed;
+        a.mlp_threshold = c->mlp_threshold;
+        a.band = c->mlp_band;
+        a.band_hi = c->mlp_band_hi;
+        a.collect = c->collect;
+        a.keep24 = c->keep24;
+        a.sample_cap = c->collect_cap;
+        a.sample_count = c->sample_count;
+        a.sample_x = c->sample_x;
+        a.sample_group = c->sample_group;
+        a.sample_node = c->sample_node;
+        a.sample_amin = c->sample_amin;
+        switch (v) {
+        case 0: return launch<false, false, 3>(c, a, 12);
+        case 1: return launch<false, true, 3>(c, a, 13);
+        case 2: return launch<true, false, 3>(c, a, 14);
+        default: return launch<true, true, 3>(c, a, 15);
+        }
+    }
+    if (c->criterion == HC_CRITERION_ERROR) {
+        a.tol2d = 1.0;      // fallback geometric rule (no previous accelerations): theta = 1
+        a.tol2f = 1.0f;
+        switch (v) {
+        case 0: return launch<false, false, 2>(c, a, 8);
+        case 1: return launch<false, true, 2>(c, a, 9);
+        case 2: return launch<true, false, 2>(c, a, 10);
+        default: return launch<true, true, 2>(c, a, 11);
+        }
+    }
+    switch (v) {
+    case 0: return launch<false, false, 0>(c, a, 0);
+    case 1: return launch<false, true, 0>(c, a, 1);
+    case 2: return launch<true, false, 0>(c, a, 2);
+    default: return launch<true, true, 0>(c, a, 3);
+    }
 }
 
 int hc_walk_setup(hc_ctx *c)
 {
-    int r = configure<false, false>(c, 0);
-    if (r == HC_OK) r = configure<false, true>(c, 1);
-    if (r == HC_OK) r = configure<true, false>(c, 2);
-    if (r == HC_OK) r = configure<true, true>(c, 3);
+    int r = configure<false, false, 0>(c, 0);
+    if (r == HC_OK) r = configure<false, true, 0>(c, 1);
+    if (r == HC_OK) r = configure<true, false, 0>(c, 2);
+    if (r == HC_OK) r = configure<true, true, 0>(c, 3);
+    if (r == HC_OK) r = configure<false, false, 1>(c, 4);
+    if (r == HC_OK) r = configure<false, true, 1>(c, 5);
+    if (r == HC_OK) r = configure<true, false, 1>(c, 6);
+    if (r == HC_OK) r = configure<true, true, 1>(c, 7);
+    if (r == HC_OK) r = configure<false, false, 2>(c, 8);
+    if (r == HC_OK) r = configure<false, true, 2>(c, 9);
+    if (r == HC_OK) r = configure<true, false, 2>(c, 10);
+    if (r == HC_OK) r = configure<true, true, 2>(c, 11);
+    if (r == HC_OK) r = configure<false, false, 3>(c, 12);
+    if (r == HC_OK) r = configure<false, true, 3>(c, 13);
+    if (r == HC_OK) r = configure<true, false, 3>(c, 14);
+    if (r == HC_OK) r = configure<true, true, 3>(c, 15);
     return r;
+}
+
+// ---------------- labels for the learned criterion ----------------
+// For each sampled (group, cell) pair: the cell's multipole acceleration at
+// every body of the group against a refined reference -- the cell's subtree
+// walked with one decision per group, a node accepted only when its mass
+// radius b satisfies b / (dmin - b) < 0.1 (so the reference's own truncation
+// error is ~1e-3 of the cell's).  label = 1 if the largest relative error
+// |a_multipole - a_reference| / |a_body| of the group is at most eps.
+namespace {
+constexpr int LSTACK = 256;
+template <bool QUAD>
+__global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, const int *gcount, const uint32_t *tord,
+                                               const double *px, const double *py, const double *pz,
+                                               const double *ax, const double *ay, const double *az,
+                                               const int *sample_group, const int *sample_node, int nsample,
+                                               float eps_label, float *y, float *rel_out)
+{
+    __shared__ int stk[4][LSTACK];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 4 + w;
+    if (i >= nsample) return;
+    const int grp = sample_group[i], node = sample_node[i];
+    const int s0 = gstart[grp], cnt = gcount[grp];
+    const bool valid = lane < cnt;
+    const uint32_t o = tord[valid ? s0 + lane : s0];
+    const double xd = px[o], yd = py[o], zd = pz[o];
+    const double gx = 0.5 * (wmind(xd) + wmaxd(xd)), gy = 0.5 * (wmind(yd) + wmaxd(yd)),
+                 gz = 0.5 * (wmind(zd) + wmaxd(zd));
+    const float ghx = __double2float_rn(gx), ghy = __double2float_rn(gy), ghz = __double2float_rn(gz);
+    const float glx = __double2float_rn(gx - (double)ghx), gly = __double2float_rn(gy - (double)ghy),
+                glz = __double2float_rn(gz - (double)ghz);
+    const float bx = __double2float_rn(xd - gx), by = __double2float_rn(yd - gy), bz = __double2float_rn(zd - gz);
+    const float gminx = wmin(bx), gmaxx = wmax(bx), gminy = wmin(by), gmaxy = wmax(by), gminz = wmin(bz),
+                gmaxz = wmax(bz);
+    const float eps2 = g.eps2f;
+    const float amag = (float)sqrt(ax[o] * ax[o] + ay[o] * ay[o] + az[o] * az[o]);
+    auto rel_pos = [&](int k, float &cx, float &cy, float &cz) {
+        const float4 A = g.nodeA[k], B = g.nodeB[k];
+        cx = (A.x - ghx) + (B.x - glx);
+        cy = (A.y - ghy) + (B.y - gly);
+        cz = (A.z - ghz) + (B.z - glz);
+        return A.w;
+    };
+    // multipole of the sampled cell
+    float mphi = 0.f, max_ = 0.f, may = 0.f, maz = 0.f;
+    {
+        float cx, cy, cz;
+        const float m = rel_pos(node, cx, cy, cz);
+        const float4 Q0 = g.nodeQ[2 * (int64_t)node], Q1 = g.nodeQ[2 * (int64_t)node + 1];
+        cell_term<QUAD>(make_float4(cx, cy, cz, m), Q0, Q1.x, Q1.y, valid, bx, by, bz, eps2, mphi, max_, may, maz);
+    }
+    // refined reference over the subtree
+    float rphi = 0.f, rax = 0.f, ray = 0.f, raz = 0.f;
+    int sp = 0;
+    {
+        const int2 C = g.nodeC[node];
+        const int nc = C.y & 255;
+        if (lane < nc) stk[w][lane] = C.x + lane;
+        sp = nc;
+    }
+    __syncwarp();
+    int guard = 0;
+    while (sp > 0 && guard < (1 << 22)) {
+        guard++;
+        const int k = stk[w][sp - 1];
+        sp--;
+        __syncwarp();
+        const int2 C = g.nodeC[k];
+        float cx, cy, cz;
+        const float m = rel_pos(k, cx, cy, cz);
+        if (C.x < 0) {
+            cell_term<false>(make_float4(cx, cy, cz, m), make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, valid, bx, by, bz,
+                             eps2, rphi, rax, ray, raz);
+            continue;
+        }
+        const float ex = fmaxf(0.f, fmaxf(gminx - cx, cx - gmaxx)), ey = fmaxf(0.f, fmaxf(gminy - cy, cy - gmaxy)),
+                    ez = fmaxf(0.f, fmaxf(gminz - cz, cz - gmaxz));
+        const float dmin = sqrtf(ex * ex + ey * ey + ez * ez);
+        const float4 Q1 = g.nodeQ[2 * (int64_t)k + 1];
+        const float b = Q1.w;
+        if (dmin - b > 10.f * b) {
+            cell_term<QUAD>(make_float4(cx, cy, cz, m), g.nodeQ[2 * (int64_t)k], Q1.x, Q1.y, valid, bx, by, bz, eps2,
+                            rphi, rax, ray, raz);
+        } else {
+            const int nc = C.y & 255;
+            if (sp + nc > LSTACK) break;          // cannot happen for depth <= 31; stop rather than overflow
+            if (lane < nc) stk[w][sp + lane] = C.x + lane;
+            sp += nc;
+            __syncwarp();
+        }
+    }
+    const float dx = max_ - rax, dy = may - ray, dz = maz - raz;
+    const float rel = valid && amag > 0.f ? sqrtf(dx * dx + dy * dy + dz * dz) / amag : 0.f;
+    const float rmax = wmax(rel);
+    if (lane == 0) {
+        y[i] = rmax <= eps_label ? 1.f : 0.f;
+        rel_out[i] = rmax;
+    }
+}
+}  // namespace
+
+int hc_label_launch(hc_ctx *c, int nsample, float eps_label)
+{
+    if (nsample <= 0) return HC_OK;
+    WalkArgs a;
+    memset(&a, 0, sizeof a);
+    a.nodeA = c->nodeA;
+    a.nodeB = c->nodeB;
+    a.nodeQ = c->nodeQ;
+    a.nodeC = c->nodeC;
+    a.eps2f = (float)(c->prm.eps * c->prm.eps);
+    const int blocks = (nsample + 3) / 4;
+    if (c->prm.usequad)
+        k_label<true><<<blocks, 128, 0, c->stream>>>(a, c->gstart, c->gcount, c->tord, c->px, c->py, c->pz, c->ax,
+                                                     c->ay, c->az, c->sample_group, c->sample_node, nsample, eps_label,
+                                                     c->sample_y, c->sample_rel);
+    else
+        k_label<false><<<blocks, 128, 0, c->stream>>>(a, c->gstart, c->gcount, c->tord, c->px, c->py, c->pz, c->ax,
+                                                      c->ay, c->az, c->sample_group, c->sample_node, nsample,
+                                                      eps_label, c->sample_y, c->sample_rel);
+    c->launches++;
+    return HC_OK;
 }

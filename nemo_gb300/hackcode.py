@@ -28,7 +28,10 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
            "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_make_testdata",
            "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate",
-           "hc_set_graphs", "hc_diagnostics_noalloc"]
+           "hc_set_graphs", "hc_diagnostics_noalloc", "hc_set_criterion", "hc_set_grouping",
+           "hc_learn_nparams", "hc_learn_init", "hc_learn_set_params", "hc_learn_get_params", "hc_learn_infer",
+           "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
+           "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band"]
 
 
 class HCError(RuntimeError):
@@ -51,7 +54,7 @@ class Diag(C.Structure):
 class WalkStats(C.Structure):
     _fields_ = [("candidates", C.c_int64), ("mixed", C.c_int64), ("entries_body", C.c_int64),
                 ("entries_cell", C.c_int64), ("borderline", C.c_int64), ("max_stack", C.c_int64),
-                ("mask_hist", C.c_int64 * 33)]
+                ("network", C.c_int64), ("network_rounds", C.c_int64), ("mask_hist", C.c_int64 * 33)]
 
     def as_dict(self):
         d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "mask_hist"}
@@ -98,6 +101,22 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_dump_tree.argtypes = [_vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]
     L.hc_forces.argtypes = [_vp]
     L.hc_evaluate.argtypes = [_vp]
+    L.hc_set_criterion.argtypes = [_vp, C.c_int, C.c_double]
+    L.hc_set_grouping.argtypes = [_vp, C.c_int]
+    _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+    L.hc_learn_nparams.argtypes = []
+    L.hc_learn_init.argtypes = [_vp, C.c_uint64]
+    L.hc_learn_set_params.argtypes = [_vp, _fp, C.c_int]
+    L.hc_learn_get_params.argtypes = [_vp, _fp, C.c_int]
+    L.hc_learn_infer.argtypes = [_vp, _fp, C.c_int64, _fp]
+    L.hc_learn_gradient.argtypes = [_vp, _fp, _fp, _vp, C.c_int64, _fp, C.POINTER(C.c_float)]
+    L.hc_learn_collect.argtypes = [_vp, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
+    L.hc_learn_samples.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.hc_learn_load_samples.argtypes = [_vp, _fp, _fp, _vp, C.c_int64]
+    L.hc_learn_train.argtypes = [_vp, C.c_int, C.c_int, C.c_double, C.c_uint64, C.POINTER(C.c_double)]
+    L.hc_learn_set_threshold.argtypes = [_vp, C.c_double]
+    L.hc_learn_relabel.argtypes = [_vp, C.c_double]
+    L.hc_learn_set_band.argtypes = [_vp, C.c_double, C.c_double]
     L.hc_diagnostics_noalloc.argtypes = [C.c_int64] + [_vp] * 13
     L.hc_set_graphs.argtypes = [_vp, C.c_int]
     L.hc_forces_at.argtypes = [_vp, _dp, C.c_int64, _dp, _dp]
@@ -236,6 +255,84 @@ class Context:
 
     def forces(self):
         self._check(self._L.hc_forces(self._h))
+
+    def set_criterion(self, criterion: str = "body", theta: float = 0.0):
+        """'body' (the reference's per-body rule) or 'group' (one decision per 32-body group at theta)."""
+        code = {"body": 0, "group": 1, "error": 2, "learned": 3}[criterion]
+        self._check(self._L.hc_set_criterion(self._h, code, float(theta)))
+
+    def set_grouping(self, kind: str = "consecutive"):
+        """Walk groups: 'consecutive' (32 bodies in key order) or 'tree' (cells of <= 32 bodies)."""
+        self._check(self._L.hc_set_grouping(self._h, {"consecutive": 0, "tree": 1}[kind]))
+
+    # ---- learned opening criterion ----
+    def learn_init(self, seed: int = 1):
+        self._check(self._L.hc_learn_init(self._h, int(seed)))
+
+    def learn_params(self, params=None):
+        n = self._L.hc_learn_nparams()
+        if params is None:
+            out = np.zeros(n, np.float32)
+            self._check(self._L.hc_learn_get_params(self._h, out, n))
+            return out
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self._L.hc_learn_set_params(self._h, p, len(p)))
+
+    def learn_infer(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 12)
+        out = np.zeros(len(x), np.float32)
+        self._check(self._L.hc_learn_infer(self._h, x, len(x), out))
+        return out
+
+    def learn_gradient(self, x, y, w=None):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 12)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        wp = None
+        if w is not None:
+            w = np.ascontiguousarray(w, dtype=np.float32)
+            wp = w.ctypes.data_as(C.c_void_p)
+        g = np.zeros(self._L.hc_learn_nparams(), np.float32)
+        loss = C.c_float()
+        self._check(self._L.hc_learn_gradient(self._h, x, y, wp, len(x), g, C.byref(loss)))
+        return loss.value, g
+
+    def learn_collect(self, theta: float, target: int) -> int:
+        n = C.c_int64()
+        self._check(self._L.hc_learn_collect(self._h, float(theta), int(target), C.byref(n)))
+        return n.value
+
+    def learn_samples(self):
+        n = C.c_int64()
+        self._check(self._L.hc_learn_samples(self._h, None, None, None, 0, C.byref(n)))
+        k = n.value
+        x = np.zeros((k, 12), np.float32)
+        y = np.zeros(k, np.float32)
+        r = np.zeros(k, np.float32)
+        self._check(self._L.hc_learn_samples(self._h, _ptr(x), _ptr(y), _ptr(r), k, C.byref(n)))
+        return x, y, r
+
+    def learn_load_samples(self, x, y, w=None):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 12)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        wp = None
+        if w is not None:
+            w = np.ascontiguousarray(w, dtype=np.float32)
+            wp = w.ctypes.data_as(C.c_void_p)
+        self._check(self._L.hc_learn_load_samples(self._h, x, y, wp, len(x)))
+
+    def learn_train(self, epochs=20, batch=4096, lr=1e-3, seed=1) -> float:
+        loss = C.c_double()
+        self._check(self._L.hc_learn_train(self._h, int(epochs), int(batch), float(lr), int(seed), C.byref(loss)))
+        return loss.value
+
+    def learn_relabel(self, rel_threshold: float):
+        self._check(self._L.hc_learn_relabel(self._h, float(rel_threshold)))
+
+    def learn_band(self, lo: float, hi: float):
+        self._check(self._L.hc_learn_set_band(self._h, float(lo), float(hi)))
+
+    def learn_threshold(self, t: float):
+        self._check(self._L.hc_learn_set_threshold(self._h, float(t)))
 
     def evaluate(self):
         """build_tree + forces as one CUDA-graph replay."""
