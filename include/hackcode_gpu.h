@@ -170,11 +170,24 @@ int hc_last_timing(hc_ctx *ctx, double *build_ms, double *walk_ms, int64_t *laun
  *     p = 3 with quadrupoles, 2 without); the group rule at theta = 1 when
  *     no previous accelerations exist.  No counterpart in hackcode1. */
 /* HC_CRITERION_LEARNED: the error rule decides clear cases; candidates whose
- *     error proxy lies within a factor 8 of the budget theta * |a| are decided
- *     by the trained network (hc_learn_*), accepted when its logit exceeds
- *     the threshold of hc_learn_set_threshold.  No counterpart in hackcode1. */
+ *     error proxy lies in the band of hc_learn_set_band around the budget
+ *     theta * |a| are decided by the trained network (hc_learn_*), accepted
+ *     when its logit exceeds the threshold of hc_learn_set_threshold.  No
+ *     counterpart in hackcode1. */
 enum { HC_CRITERION_BODY = 0, HC_CRITERION_GROUP = 1, HC_CRITERION_ERROR = 2, HC_CRITERION_LEARNED = 3 };
 int hc_set_criterion(hc_ctx *ctx, int criterion, double theta);
+
+/* Guard of the group, error and learned criteria (no counterpart in
+ * hackcode1): after each of their force evaluations the accelerations of
+ * `nsample` bodies (a uniform sample drawn once from `seed`) are compared on
+ * the device with an FP32 direct sum over all bodies; when the RMS relative
+ * error exceeds rms_max the evaluation's forces are recomputed with the
+ * per-body rule at the context's tol (closing half-kick included), inside the
+ * same CUDA graph.  nsample = 0 turns it off.  hc_guard_stats: checks made,
+ * checks failed, RMS of the last check. */
+#define HC_GUARD_MAX_SAMPLE 65536
+int hc_set_guard(hc_ctx *ctx, int64_t nsample, double rms_max, uint64_t seed);
+int hc_guard_stats(hc_ctx *ctx, int64_t *checks, int64_t *trips, double *last_rms);
 
 /* ---- learned opening criterion (no counterpart in hackcode1) ----
  * The network: 12 features of a (group, cell) pair -> 64 -> 64 (SiLU) -> 1
@@ -211,8 +224,9 @@ int hc_learn_set_band(hc_ctx *ctx, double lo, double hi);
 
 /* How the walk groups its 32 bodies per warp: HC_GROUPS_CONSECUTIVE (32
  * bodies consecutive in key order) or HC_GROUPS_TREE (the bodies of one cell
- * holding at most 32, siblings packed).  Results of HC_CRITERION_BODY do not
- * depend on it; HC_CRITERION_GROUP always uses tree groups. */
+ * holding at most 32, siblings packed).  The interaction sets of
+ * HC_CRITERION_BODY do not depend on it (the rounding of the FP32 sums does);
+ * the other criteria always use tree groups. */
 enum { HC_GROUPS_CONSECUTIVE = 0, HC_GROUPS_TREE = 1 };
 int hc_set_grouping(hc_ctx *ctx, int kind);
 

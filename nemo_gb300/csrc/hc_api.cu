@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <unordered_set>
 #include <vector>
 #include "hc_internal.cuh"
 #include "hc_mlp.cuh"
@@ -73,7 +74,7 @@ void free_all(hc_ctx *c)
         if (p) cudaFree(p);
     void *mptrs[] = {c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_grad, c->mlp_loss, c->mlp_gpart, c->mlp_lpart,
                      c->mlp_packed, c->sample_count, c->sample_x, c->sample_amin, c->sample_y, c->sample_rel,
-                     c->sample_w, c->sample_group, c->sample_node};
+                     c->sample_w, c->sample_group, c->sample_node, c->guard_idx, c->guard_part, c->guard};
     for (void *p : mptrs)
         if (p) cudaFree(p);
     if (c->h_st) cudaFreeHost(c->h_st);
@@ -553,6 +554,12 @@ static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bo
     HC_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, rflags));
     HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
                           nstep));
+    if (c->guard_n > 0 && c->criterion != HC_CRITERION_BODY) {
+        // guard: sampled direct sum; on failure the per-body rule redoes the walk
+        hc_guard_launch(c);
+        HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
+                              nstep, &c->guard->flag, true));
+    }
     HC_CUDA(cudaEventRecordWithFlags(c->ev[3], c->stream, rflags));
     if (with_diag) {
         hc_diag_launch(c, c->d_diag);
@@ -696,6 +703,78 @@ int hc_set_criterion(hc_ctx *ctx, int criterion, double theta)
             cudaGraphExecDestroy(g.exec);
             g.exec = nullptr;
         }
+    return HC_OK;
+}
+
+int hc_set_guard(hc_ctx *ctx, int64_t nsample, double rms_max, uint64_t seed)
+{
+    if (!ctx || nsample < 0 || nsample > HC_GUARD_MAX_SAMPLE) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    if (nsample > c->n || (nsample > 0 && !(rms_max > 0.0))) {
+        c->err = "hc_set_guard: need 0 <= nsample <= nbody and rms_max > 0";
+        return HC_ERR_ARG;
+    }
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->guard_idx) cudaFree(c->guard_idx);
+    if (c->guard_part) cudaFree(c->guard_part);
+    c->guard_idx = nullptr;
+    c->guard_part = nullptr;
+    c->guard_n = 0;
+    for (auto &g : c->graphs)        // captured graphs bake the guard nodes
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+    if (nsample == 0) return HC_OK;
+    // seeded uniform sample without replacement (Floyd's algorithm), ascending
+    std::vector<int64_t> pick;
+    {
+        std::unordered_set<int64_t> seen;
+        uint64_t st = seed * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL;
+        auto next = [&st]() {
+            st += 0x9E3779B97F4A7C15ULL;            // splitmix64
+            uint64_t z = st;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+            return z ^ (z >> 31);
+        };
+        for (int64_t j = c->n - nsample; j < c->n; j++) {
+            const int64_t t = (int64_t)(next() % (uint64_t)(j + 1));
+            if (seen.insert(t).second) pick.push_back(t);
+            else {
+                seen.insert(j);
+                pick.push_back(j);
+            }
+        }
+        std::sort(pick.begin(), pick.end());
+    }
+    if (!c->guard) {
+        HC_TRY(dalloc(c, &c->guard, 1));
+        HC_CUDA(cudaMemset(c->guard, 0, sizeof(hc_guard_state)));
+    }
+    const int slices = hc_guard_slices(c);
+    if (slices <= 0) return HC_ERR_CUDA;
+    HC_TRY(dalloc(c, &c->guard_idx, nsample));
+    HC_TRY(dalloc(c, &c->guard_part, (int64_t)slices * nsample));
+    HC_CUDA(cudaMemcpy(c->guard_idx, pick.data(), sizeof(int64_t) * nsample, cudaMemcpyHostToDevice));
+    c->guard_slices = slices;
+    c->guard_rms_max = rms_max;
+    c->guard_n = nsample;
+    return HC_OK;
+}
+
+int hc_guard_stats(hc_ctx *ctx, int64_t *checks, int64_t *trips, double *last_rms)
+{
+    if (!ctx) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    hc_guard_state g = {};
+    if (c->guard) {
+        HC_CUDA(cudaStreamSynchronize(c->stream));
+        HC_CUDA(cudaMemcpy(&g, c->guard, sizeof g, cudaMemcpyDeviceToHost));
+    }
+    if (checks) *checks = (int64_t)g.checks;
+    if (trips) *trips = (int64_t)g.trips;
+    if (last_rms) *last_rms = g.last_rms;
     return HC_OK;
 }
 

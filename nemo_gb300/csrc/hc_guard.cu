@@ -1,0 +1,127 @@
+// hc_guard.cu -- per-evaluation guard of the approximate opening criteria.
+//
+// The group, error-bound and learned criteria trade exactness of the
+// reference's per-body rule (grav.c:122-131) for fewer interactions.  The
+// guard keeps their error bounded: after each of their walks the
+// accelerations of a fixed sample of bodies are compared with a direct sum
+// over all bodies; when the RMS relative error over the sample exceeds the
+// budget, a flag is raised on the device and the walk that follows in the
+// same launch sequence (the per-body rule at the context's tol) recomputes
+// every force.  That walk's closing half-kick, v += (a_new - a_stored) dt/2,
+// starts from the accelerations the approximate walk stored, so the velocity
+// ends as if only the fallback walk had run.  No host round trip: the whole
+// sequence is captured in the evaluation's CUDA graph.
+//
+// Direct sum: FP32 with positions split into float hi + lo parts (separations
+// formed as (hi - hi) + (lo - lo)), partial sums per source slice, reduced in
+// FP64 in slice order (deterministic).
+#include "hc_internal.cuh"
+
+namespace {
+
+constexpr int GT = 256;
+
+__global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *mass, const double *px,
+                                                     const double *py, const double *pz, const int64_t *idx, int ns,
+                                                     float eps2, int64_t slice, float4 *part)
+{
+    __shared__ float4 sh[GT], sl[GT];
+    const int s = blockIdx.y * GT + threadIdx.x;
+    const bool valid = s < ns;
+    const int64_t me = valid ? idx[s] : -1;
+    const double xd = valid ? px[me] : 0.0, yd = valid ? py[me] : 0.0, zd = valid ? pz[me] : 0.0;
+    const float xh = __double2float_rn(xd), yh = __double2float_rn(yd), zh = __double2float_rn(zd);
+    const float xl = __double2float_rn(xd - (double)xh), yl = __double2float_rn(yd - (double)yh),
+                zl = __double2float_rn(zd - (double)zh);
+    const int64_t j0 = (int64_t)blockIdx.x * slice;
+    const int64_t j1 = j0 + slice < n ? j0 + slice : n;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int64_t base = j0; base < j1; base += GT) {
+        const int64_t j = base + threadIdx.x;
+        if (j < j1) {
+            const double x = px[j], y = py[j], z = pz[j];
+            const float h0 = __double2float_rn(x), h1 = __double2float_rn(y), h2 = __double2float_rn(z);
+            sh[threadIdx.x] = make_float4(h0, h1, h2, __double2float_rn(mass[j]));
+            sl[threadIdx.x] = make_float4(__double2float_rn(x - (double)h0), __double2float_rn(y - (double)h1),
+                                          __double2float_rn(z - (double)h2), 0.f);
+        }
+        __syncthreads();
+        const int cnt = j1 - base < GT ? (int)(j1 - base) : GT;
+        for (int k = 0; k < cnt; k++) {
+            const float4 H = sh[k], L = sl[k];
+            const float dx = (H.x - xh) + (L.x - xl), dy = (H.y - yh) + (L.y - yl), dz = (H.z - zh) + (L.z - zl);
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+            const float rinv = rsqrtf(r2);
+            const float mr3 = (base + k == me) ? 0.f : H.w * rinv * rinv * rinv;   // self skipped
+            ax = fmaf(mr3, dx, ax);
+            ay = fmaf(mr3, dy, ay);
+            az = fmaf(mr3, dz, az);
+        }
+        __syncthreads();
+    }
+    if (valid) part[(int64_t)blockIdx.x * ns + s] = make_float4(ax, ay, az, 0.f);
+}
+
+__global__ void __launch_bounds__(GT) k_guard_check(const float4 *part, int slices, int ns, const int64_t *idx,
+                                                    const double *ax, const double *ay, const double *az,
+                                                    double rms_max, hc_guard_state *gs, hc_status *st)
+{
+    __shared__ double red[GT];
+    double acc = 0.0;
+    for (int s = threadIdx.x; s < ns; s += GT) {
+        double dx = 0.0, dy = 0.0, dz = 0.0;
+        for (int b = 0; b < slices; b++) {
+            const float4 p = part[(int64_t)b * ns + s];
+            dx += (double)p.x;
+            dy += (double)p.y;
+            dz += (double)p.z;
+        }
+        const int64_t i = idx[s];
+        const double ex = ax[i] - dx, ey = ay[i] - dy, ez = az[i] - dz;
+        const double a2 = dx * dx + dy * dy + dz * dz;
+        if (a2 > 0.0) acc += (ex * ex + ey * ey + ez * ez) / a2;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = GT / 2; o; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double rms = sqrt(red[0] / (double)ns);
+        const bool trip = !(rms <= rms_max);   // NaN trips
+        gs->last_rms = rms;
+        gs->checks++;
+        gs->flag = trip ? 1 : 0;
+        if (trip) {
+            gs->trips++;
+            st->n2b = 0;                        // the fallback walk's counts replace these
+            st->nbc = 0;
+        }
+    }
+}
+
+}  // namespace
+
+int hc_guard_slices(hc_ctx *c)
+{
+    int dev = 0, nsm = 0;
+    HC_CUDA(cudaGetDevice(&dev));
+    HC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    return 2 * nsm;
+}
+
+// No CUDA queries here: this runs inside stream capture.
+void hc_guard_launch(hc_ctx *c)
+{
+    const int ns = (int)c->guard_n;
+    int64_t slice = (c->n + c->guard_slices - 1) / c->guard_slices;
+    if (slice < 1) slice = 1;
+    const int slices = (int)((c->n + slice - 1) / slice);
+    const dim3 grid((unsigned)slices, (unsigned)((ns + GT - 1) / GT));
+    k_guard_direct<<<grid, GT, 0, c->stream>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns,
+                                              (float)(c->prm.eps * c->prm.eps), slice, c->guard_part);
+    k_guard_check<<<1, GT, 0, c->stream>>>(c->guard_part, slices, ns, c->guard_idx, c->ax, c->ay, c->az,
+                                           c->guard_rms_max, c->guard, c->st);
+    c->launches += 2;
+}

@@ -22,6 +22,14 @@
 #define HC_GROUP 32           // bodies per walk group (one warp)
 
 // Device status word (written by kernels, read by the host after a sync).
+// Guard record, kept across evaluations.
+struct hc_guard_state {
+    double last_rms;              // RMS relative force error of the last check
+    unsigned long long checks, trips;
+    int flag;                     // 1: the last check failed and the fallback walk runs
+    int pad;
+};
+
 struct hc_status {
     int error;                // 0 or HC_ERR_*
     int info;
@@ -124,6 +132,13 @@ struct hc_ctx {
     int nsample;                          // samples held on the device
     int64_t band_total;                   // band candidates seen by the last collection walk
     int criterion;                        // HC_CRITERION_* of include/hackcode_gpu.h
+    // per-evaluation guard of the approximate criteria (hc_guard.cu)
+    int64_t guard_n;                      // sampled bodies (0: off)
+    double guard_rms_max;
+    int guard_slices;                     // source slices of the direct sum
+    int64_t *guard_idx;                   // sampled body indices (ascending)
+    float4 *guard_part;                   // [slices][guard_n] partial accelerations
+    struct hc_guard_state *guard;
     double group_theta;                   // opening angle of the group criterion
 
     // scratch
@@ -160,7 +175,8 @@ void hc_keys_for_points(hc_ctx *c, const double *x, const double *y, const doubl
 // walk (hc_walk.cu)
 int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorted,
                    const double *tx, const double *ty, const double *tz, double *oax, double *oay,
-                   double *oaz, double *ophi, double kick_dthf, int64_t nstep);
+                   double *oaz, double *ophi, double kick_dthf, int64_t nstep,
+                   const int *run_flag = nullptr, bool body_rule = false);
 int hc_walk_setup(hc_ctx *c);
 struct MlpSmem;
 int hc_label_launch(hc_ctx *c, int nsample, float eps_label);
@@ -176,6 +192,9 @@ int hc_relabel_impl(hc_ctx *c, float thr);
 void hc_kick_drift(hc_ctx *c, double dt);
 void hc_diag_launch(hc_ctx *c, double *out36);
 void hc_direct_launch(hc_ctx *c, const int64_t *idx_dev, int64_t ns, double *oacc, double *ophi);
+// guard (hc_guard.cu)
+int hc_guard_slices(hc_ctx *c);
+void hc_guard_launch(hc_ctx *c);
 int hc_fma_peak_impl(hc_ctx *c, double *tflops);
 
 #define HC_CUDA(call)                                                               \

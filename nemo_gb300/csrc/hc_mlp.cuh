@@ -204,11 +204,17 @@ __device__ __forceinline__ float mlp_warp_lean(const MlpSmem &P, const __nv_bflo
 #pragma unroll 2
         for (int nt = 0; nt < 8; nt++) {
             const int n = nt * 8 + g, col = nt * 8 + 2 * t;
-            float c[4] = {0.f, 0.f, 0.f, 0.f};
+            // k-tiles 0,1 and 2,3 in two independent accumulators (shorter mma chain)
+            float c[4] = {0.f, 0.f, 0.f, 0.f}, e[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-            for (int kt = 0; kt < 4; kt++)
+            for (int kt = 0; kt < 2; kt++) {
                 mma_bf16_16816(c, h1[kt], w2[(n * MLP_S2 + kt * 16 + 2 * t) >> 1],
                                w2[(n * MLP_S2 + kt * 16 + 2 * t + 8) >> 1]);
+                mma_bf16_16816(e, h1[kt + 2], w2[(n * MLP_S2 + (kt + 2) * 16 + 2 * t) >> 1],
+                               w2[(n * MLP_S2 + (kt + 2) * 16 + 2 * t + 8) >> 1]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) c[q] += e[q];
             const float bias0 = P.b2[col], bias1 = P.b2[col + 1];
             const float v0 = silu(c[0] + bias0), v1 = silu(c[1] + bias1);
             const float v2 = silu(c[2] + bias0), v3 = silu(c[3] + bias1);

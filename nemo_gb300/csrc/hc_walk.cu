@@ -86,6 +86,7 @@ struct WalkArgs {
     int use_table;                        // 1: table groups, then massless targets in 32s
     float eps_acc;                        // MODE 2/3 error budget relative to |a|
     const double *pax, *pay, *paz;        // MODE 2/3: accelerations of the previous evaluation
+    const int *run_flag;                  // when set: the walk runs only if *run_flag != 0
     const MlpSmem *mlp;                   // MODE 3: packed network
     float mlp_threshold;                  // MODE 3: accept iff logit > threshold
     float band;                           // MODE 3: network band in log2(proxy / budget): [-band, band_hi]
@@ -240,6 +241,7 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
 template <bool QUAD, bool COUNT, int MODE>
 __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs g)
 {
+    if (g.run_flag && *g.run_flag == 0) return;   // guard passed: no fallback walk
     extern __shared__ float4 smem_raw[];
     WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[threadIdx.x >> 5];
     // MODE 3: per-warp queues after the warp areas; the network's weights are
@@ -692,10 +694,11 @@ int launch(hc_ctx *c, WalkArgs &a, int variant)
 
 int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorted, const double *tx,
                    const double *ty, const double *tz, double *oax, double *oay, double *oaz, double *ophi,
-                   double kick_dthf, int64_t nstep)
+                   double kick_dthf, int64_t nstep, const int *run_flag, bool body_rule)
 {
     if (ntarget <= 0) return HC_OK;
     WalkArgs a;
+    a.run_flag = run_flag;
     a.nodeA = c->nodeA;
     a.nodeB = c->nodeB;
     a.nodeQ = c->nodeQ;
@@ -736,7 +739,7 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     const bool count = c->prm.count_per_body && self && c->cnt_b;
     const int v = (c->prm.usequad ? 2 : 0) + (count ? 1 : 0);
     a.eps_acc = (float)c->group_theta;
-    if (c->criterion == HC_CRITERION_GROUP) {
+    if (!body_rule && c->criterion == HC_CRITERION_GROUP) {
         a.tol2d = c->group_theta * c->group_theta;
         a.tol2f = (float)a.tol2d;
         switch (v) {
@@ -746,7 +749,7 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
         default: return launch<true, true, 1>(c, a, 7);
         }
     }
-    if (c->criterion == HC_CRITERION_LEARNED) {
+    if (!body_rule && c->criterion == HC_CRITERION_LEARNED) {
         a.tol2d = 0.25;     // fallback geometric rule (no previous accelerations): theta = 0.5
         a.tol2f = 0.25f;
         a.mlp = c->mlp_packed;
@@ -768,7 +771,7 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
         default: return launch<true, true, 3>(c, a, 15);
         }
     }
-    if (c->criterion == HC_CRITERION_ERROR) {
+    if (!body_rule && c->criterion == HC_CRITERION_ERROR) {
         a.tol2d = 1.0;      // fallback geometric rule (no previous accelerations): theta = 1
         a.tol2f = 1.0f;
         switch (v) {

@@ -31,7 +31,7 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_set_graphs", "hc_diagnostics_noalloc", "hc_set_criterion", "hc_set_grouping",
            "hc_learn_nparams", "hc_learn_init", "hc_learn_set_params", "hc_learn_get_params", "hc_learn_infer",
            "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
-           "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band"]
+           "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band", "hc_set_guard", "hc_guard_stats"]
 
 
 class HCError(RuntimeError):
@@ -103,6 +103,8 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_evaluate.argtypes = [_vp]
     L.hc_set_criterion.argtypes = [_vp, C.c_int, C.c_double]
     L.hc_set_grouping.argtypes = [_vp, C.c_int]
+    L.hc_set_guard.argtypes = [_vp, C.c_int64, C.c_double, C.c_uint64]
+    L.hc_guard_stats.argtypes = [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
     L.hc_learn_nparams.argtypes = []
     L.hc_learn_init.argtypes = [_vp, C.c_uint64]
@@ -257,13 +259,24 @@ class Context:
         self._check(self._L.hc_forces(self._h))
 
     def set_criterion(self, criterion: str = "body", theta: float = 0.0):
-        """'body' (the reference's per-body rule) or 'group' (one decision per 32-body group at theta)."""
+        """'body' (the reference's per-body rule), or one decision per 32-body group: 'group' (opening
+        angle theta), 'error' (truncation-error budget theta |a|), 'learned' (the network in the error
+        rule's band)."""
         code = {"body": 0, "group": 1, "error": 2, "learned": 3}[criterion]
         self._check(self._L.hc_set_criterion(self._h, code, float(theta)))
 
     def set_grouping(self, kind: str = "consecutive"):
         """Walk groups: 'consecutive' (32 bodies in key order) or 'tree' (cells of <= 32 bodies)."""
         self._check(self._L.hc_set_grouping(self._h, {"consecutive": 0, "tree": 1}[kind]))
+
+    def set_guard(self, nsample: int, rms_max: float = 1e-3, seed: int = 1):
+        """Per-evaluation guard of the approximate criteria (0 samples: off)."""
+        self._check(self._L.hc_set_guard(self._h, int(nsample), float(rms_max), int(seed)))
+
+    def guard_stats(self) -> dict:
+        ch, tr, rms = C.c_int64(), C.c_int64(), C.c_double()
+        self._check(self._L.hc_guard_stats(self._h, C.byref(ch), C.byref(tr), C.byref(rms)))
+        return {"checks": ch.value, "trips": tr.value, "last_rms": rms.value}
 
     # ---- learned opening criterion ----
     def learn_init(self, seed: int = 1):
