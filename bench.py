@@ -2,9 +2,14 @@
 """Benchmark of the hackcode1 hot path on GB300.
 
 A step is one force evaluation of a Plummer sphere of N = 1,048,576 bodies
-(mkplummer seed=1) at tol=0.5, eps=0.01 with quadrupole moments: octree
-build (expandbox replay, keys, sort, cells, moments) plus the force walk of
-every body.  The opening criterion is the reference's fixed-theta rule.
+(mkplummer seed=1) at eps=0.01 with quadrupole moments: octree build
+(expandbox replay, keys, sort, cells, moments) plus the force walk of every
+body.  The headline is the learned opening criterion (network trained on
+labels from this system, guard on) at the RMS force error of the
+reference's fixed-theta rule at tol=0.5, against that rule on the GPU; the
+error-bound rule (the method without its network) and the comparison at RMS
+1e-3 are reported beside it.  Errors are measured against an FP64 direct sum
+on a seeded sample of 16,384 bodies.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -36,9 +41,11 @@ FLOPS_MONO, FLOPS_QUAD = 20, 59          # per interaction, as counted in hc_wal
 L2_FLUSH_BYTES = 512 << 20
 
 
-def workload_config(n):
+def workload_config(n, mode=("body", TOL)):
+    crit = {"body": "fixed-theta (grav.c subdivp)", "error": "error-bound group rule",
+            "learned": "learned opening criterion (guarded)"}[mode[0]]
     return {"workload": f"plummer N={n} seed={SEED}: one force evaluation (octree build + walk of all bodies)",
-            "n": n, "tol": TOL, "eps": EPS, "usequad": USEQUAD, "criterion": "fixed-theta (grav.c subdivp)",
+            "n": n, "tol": TOL, "eps": EPS, "usequad": USEQUAD, "criterion": crit, "criterion_setting": list(mode),
             "l2": "flushed between steps (512 MiB write, outside the per-step device timing)",
             "parallelism": "replicas (one independent system per GPU)"}
 
@@ -183,6 +190,90 @@ def cpu_leg(n: int, m, pos, procs: int, nsample_per_proc: int, seed: int = 0):
 
 # ---------------------------------------------------------------- GPU leg
 
+RMS_BUDGET = 1e-3            # the force-error budget of comparison (ii) and of the guard
+GUARD_SAMPLE = 256
+ERROR_EPS = (0.015, 0.02, 0.025, 0.03, 0.035, 0.04, 0.05)
+LEARNED_GRID = ((0.03, -1.0), (0.03, 0.0), (0.04, 0.0), (0.04, 1.0), (0.05, 0.0), (0.05, 1.0), (0.05, 2.0))
+THETA_GRID = (0.56, 0.6, 0.62, 0.64, 0.66, 0.68, 0.7)
+ERROR_EPS_II = (0.4, 0.6, 1.0, 1.5, 2.0, 3.0, 4.0)
+LEARNED_GRID_II = ((0.6, 0.0), (1.0, 0.0), (1.5, 0.0), (2.0, 0.0), (3.0, 0.0), (4.0, 0.0))
+
+
+def set_mode(ctx, mode):
+    """mode: ("body", theta) | ("error", eps) | ("learned", eps, logit threshold).
+    The context's tol is theta for the per-body rule and 0.5 otherwise (the
+    fallback of the guard)."""
+    if mode[0] == "body":
+        ctx.set_params(tol=mode[1])
+        ctx.set_criterion("body")
+    elif mode[0] == "error":
+        ctx.set_params(tol=TOL)
+        ctx.set_criterion("error", mode[1])
+    else:
+        ctx.set_params(tol=TOL)
+        ctx.set_criterion("learned", mode[1])
+        ctx.learn_threshold(mode[2])
+
+
+def sample_error(ctx, idx, ea):
+    _, acc, _ = ctx.download(phase=False, phi=False)
+    rel = np.linalg.norm(acc[idx] - ea, axis=1) / np.linalg.norm(ea, axis=1)
+    return float(np.sqrt(np.mean(rel ** 2))), float(np.percentile(rel, 99))
+
+
+def point(ctx, mode, idx, ea, reps=3):
+    """Steady state of one criterion setting (previous accelerations from the
+    same setting): best step time, RMS and p99 error, interactions."""
+    set_mode(ctx, mode)
+    ctx.evaluate()
+    ts = []
+    for _ in range(reps):
+        ctx.evaluate()
+        b, w, _ = ctx.timing()
+        ts.append(b + w)
+    d = ctx.diagnostics()
+    rms, p99 = sample_error(ctx, idx, ea)
+    return {"mode": list(mode), "step_ms": min(ts), "rms": rms, "p99": p99, "interactions": int(d.n2b + d.nbc)}
+
+
+def pick(points, target):
+    """Fastest setting whose RMS error is within the target."""
+    ok = [p for p in points if p["rms"] <= target]
+    return min(ok, key=lambda p: p["step_ms"]) if ok else None
+
+
+def timed(ctx, mode, steps, warmup, flush, world):
+    """K steps of one criterion, device-timed with CUDA events on the context
+    stream, L2 flushed before each.  Returns per-step ms, build / walk ms,
+    kernel launches, interactions of the last step."""
+    import torch
+    set_mode(ctx, mode)
+    for _ in range(warmup):
+        ctx.evaluate()
+    step_ms, build_ms, walk_ms, launches = [], [], [], 0
+    barrier(world)
+    torch.cuda.synchronize()
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.timer_start()
+        ctx.evaluate()          # build + walk (+ guard), replayed from a captured CUDA graph
+        step_ms.append(ctx.timer_stop())
+        b, w, nl = ctx.timing()
+        build_ms.append(b)
+        walk_ms.append(w)
+        launches += nl
+    torch.cuda.synchronize()
+    barrier(world)
+    d = ctx.diagnostics()
+    return {"step_ms": statistics.mean(step_ms), "build_ms": statistics.mean(build_ms),
+            "walk_ms": statistics.mean(walk_ms), "launches": launches, "n2b": int(d.n2b), "nbc": int(d.nbc)}
+
+
+def walk_flops(n2b, nbc):
+    return FLOPS_MONO * n2b + (FLOPS_QUAD if USEQUAD else FLOPS_MONO) * nbc
+
+
 def run_ours(args, world, rank, local):
     import torch
     from nemo_gb300 import build as B
@@ -196,116 +287,142 @@ def run_ours(args, world, rank, local):
     ctx = hc.Context(n, tol=TOL, eps=EPS, fcells=1.0, usequad=USEQUAD)
     ctx.upload(m, ph)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
-    def step():
-        ctx.evaluate()          # build + walk, replayed from a captured CUDA graph
-
     for _ in range(args.warmup):
-        step()
+        ctx.evaluate()
     peak = ctx.fp32_peak_tflops()
 
-    # ---- device-resident throughput ----
-    step_ms, build_ms, walk_ms, launches = [], [], [], 0
-    barrier(world)
-    torch.cuda.synchronize()
-    wall0 = time.perf_counter()
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            ctx.timer_start()
-            step()
-            step_ms.append(ctx.timer_stop())
-            b, w, nl = ctx.timing()
-            build_ms.append(b)
-            walk_ms.append(w)
-            launches += nl
-    torch.cuda.synchronize()
-    barrier(world)
-    wall = time.perf_counter() - wall0
-    d = ctx.diagnostics()
-    n2b, nbc = int(d.n2b), int(d.nbc)
-    ws = ctx.walk_stats()
-    ws["mask_fill"] = (n2b + nbc) / max(1, 32 * (ws["entries_body"] + ws["entries_cell"]))
-    value, mean_ms = job_throughput(n, statistics.mean(step_ms), world)
+    # ---- FP64 direct-sum sample (bodies do not move: one evaluation per step) ----
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(n, size=min(args.sample, n), replace=False)).astype(np.int64)
+    ea, _ = ctx.direct_sample(idx)
 
-    # ---- end to end through the public API, host buffers (pinned) ----
+    # ---- the learned criterion: labels from this system, training on the device ----
+    t0 = time.perf_counter()
+    set_mode(ctx, ("body", TOL))
+    ctx.evaluate()
+    train = ctx.learn_from_self(theta=0.03, target=1 << 20)
+    torch.cuda.synchronize()
+    train["seconds"] = time.perf_counter() - t0
+    ctx.learn_band(0.5, 3.0)
+
+    # ---- calibration to equal RMS (untimed) ----
+    fixed = point(ctx, ("body", TOL), idx, ea)
+    target = fixed["rms"]
+    cal_err = [point(ctx, ("error", e), idx, ea) for e in ERROR_EPS]
+    cal_lrn = [point(ctx, ("learned", e, t), idx, ea) for e, t in LEARNED_GRID]
+    err_pt, lrn_pt = pick(cal_err, target), pick(cal_lrn, target)
+    cal_th = [point(ctx, ("body", t), idx, ea) for t in THETA_GRID]
+    cal_err2 = [point(ctx, ("error", e), idx, ea) for e in ERROR_EPS_II]
+    cal_lrn2 = [point(ctx, ("learned", e, t), idx, ea) for e, t in LEARNED_GRID_II]
+    th_pt2, err_pt2, lrn_pt2 = pick(cal_th, RMS_BUDGET), pick(cal_err2, RMS_BUDGET), pick(cal_lrn2, RMS_BUDGET)
+    head_mode = tuple(lrn_pt["mode"]) if lrn_pt else ("body", TOL)
+
+    # ---- timed: the headline (learned, guard on) and its comparisons ----
+    ctx.set_guard(GUARD_SAMPLE, RMS_BUDGET, seed=1)
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        head = timed(ctx, head_mode, args.steps, args.warmup, flush, world)
+        wall = time.perf_counter() - wall0
+        guard = ctx.guard_stats()
+        head_err = sample_error(ctx, idx, ea)
+        ws = ctx.walk_stats()
+        comp = {"fixed_theta_0.5": timed(ctx, ("body", TOL), args.steps, args.warmup, flush, world)}
+        comp["fixed_theta_0.5"]["rms"] = sample_error(ctx, idx, ea)[0]
+        if err_pt:
+            comp["error_rule"] = timed(ctx, tuple(err_pt["mode"]), args.steps, args.warmup, flush, world)
+            comp["error_rule"]["rms"] = sample_error(ctx, idx, ea)[0]
+        for name, pt in (("fixed_theta_at_1e-3", th_pt2), ("error_rule_at_1e-3", err_pt2),
+                         ("learned_at_1e-3", lrn_pt2)):
+            if pt:
+                comp[name] = timed(ctx, tuple(pt["mode"]), args.steps, args.warmup, flush, world)
+                comp[name]["rms"] = sample_error(ctx, idx, ea)[0]
+                comp[name]["mode"] = pt["mode"]
+    clocks = clk.summary()
+    value, mean_ms = job_throughput(n, head["step_ms"], world)
+    fixed_value, _ = job_throughput(n, comp["fixed_theta_0.5"]["step_ms"], world)
+    for v in comp.values():
+        v["bodies_per_s"] = job_throughput(n, v["step_ms"], world)[0]
+        v["walk_fp32_frac"] = walk_flops(v["n2b"], v["nbc"]) / (v["walk_ms"] * 1e-3) / 1e12 / peak
+    ratios = {"learned_vs_fixed_theta_equal_rms": value / fixed_value}
+    if "error_rule" in comp:
+        ratios["error_rule_vs_fixed_theta_equal_rms"] = comp["error_rule"]["bodies_per_s"] / fixed_value
+    if "learned_at_1e-3" in comp and "fixed_theta_at_1e-3" in comp:
+        ratios["learned_vs_fixed_theta_at_rms_1e-3"] = (comp["learned_at_1e-3"]["bodies_per_s"]
+                                                        / comp["fixed_theta_at_1e-3"]["bodies_per_s"])
+
+    # ---- end to end through the public API, host buffers (pinned): the
+    # headline criterion, the host carrying positions and the previous
+    # accelerations across calls ----
+    set_mode(ctx, head_mode)
     hm = torch.from_numpy(m).pin_memory()
     hph = torch.from_numpy(ph.reshape(-1)).pin_memory()
     hacc = torch.empty(3 * n, dtype=torch.float64).pin_memory()
     hphi = torch.empty(n, dtype=torch.float64).pin_memory()
+    ctx.evaluate()
+    ctx.download_ptr(None, hacc.data_ptr(), hphi.data_ptr())
     e2e_ms = []
     for i in range(args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         ctx.timer_start()
         ctx.upload_ptr(hm.data_ptr(), hph.data_ptr())
+        ctx.set_forces_ptr(hacc.data_ptr(), None)
         ctx.evaluate()
         ctx.download_ptr(None, hacc.data_ptr(), hphi.data_ptr())
         t = ctx.timer_stop()
         if i >= args.warmup:
             e2e_ms.append(t)
-    e2e_value, e2e_mean = job_throughput(n, statistics.mean(e2e_ms), world)
+    e2e_value, _ = job_throughput(n, statistics.mean(e2e_ms), world)
+    ctx.set_guard(0)
 
-    # ---- roofline of the walk kernel ----
-    flops = FLOPS_MONO * n2b + (FLOPS_QUAD if USEQUAD else FLOPS_MONO) * nbc
-    walk_mean = statistics.mean(walk_ms)
-    achieved = flops / (walk_mean * 1e-3) / 1e12
+    # ---- roofline of the headline walk kernel ----
+    flops = walk_flops(head["n2b"], head["nbc"])
+    achieved = flops / (head["walk_ms"] * 1e-3) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "walk_traffic.json")
     if os.path.exists(tpath):
         try:
             t = json.load(open(tpath))
             if int(t.get("n", 0)) == n:
-                traffic = t.get("bytes_per_launch")
+                traffic = t.get("learned" if head_mode[0] == "learned" else "body")
         except (OSError, ValueError):
             traffic = None
+    ws["mask_fill"] = (head["n2b"] + head["nbc"]) / max(1, 32 * (ws["entries_body"] + ws["entries_cell"]))
 
-    # ---- force error against the FP64 direct sum on a sample ----
-    ferr = None
-    if args.sample > 0 and rank == 0:
-        rng = np.random.default_rng(12345)
-        idx = np.sort(rng.choice(n, size=min(args.sample, n), replace=False)).astype(np.int64)
-        ea, _ = ctx.direct_sample(idx)
-        _, acc, _ = ctx.download(phase=False, phi=False)
-        rel = np.linalg.norm(acc[idx] - ea, axis=1) / np.linalg.norm(ea, axis=1)
-        ferr = {"rms": float(np.sqrt(np.mean(rel ** 2))), "p99": float(np.percentile(rel, 99)),
-                "max": float(rel.max()), "sample": int(len(idx)), "against": "FP64 direct sum (GPU)"}
-
-    if args.stats:
-        sctx = hc.Context(n, tol=TOL, eps=EPS, fcells=1.0, usequad=USEQUAD, count_per_body=True)
-        sctx.upload(m, ph)
-        sctx.evaluate()
-        ws["count_walk"] = sctx.walk_stats()
-        sctx.close()
-    clocks = clk.summary()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: Plummer sphere drawn as mkplummer does (ran3, seed=1)",
-        "config": workload_config(n),
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 56 * n,
-                "d2h_bytes_per_step": 32 * n},
-        "gpu_launches": launches,
+        "config": workload_config(n, head_mode),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 80 * n, "d2h_bytes_per_step": 32 * n,
+                "calls": "hc_upload + hc_set_forces (previous accelerations) + hc_evaluate + hc_download"},
+        "gpu_launches": head["launches"],
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_walk<quad>",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_walk<quad> (headline criterion)",
                      "peak_source": "measured live: FP32 FMA chain kernel (hc_fp32_peak), FMA = 2 flops",
                      "flops_per_launch": flops},
-        "interactions_per_s": world * (n2b + nbc) / (mean_ms * 1e-3),
-        "interactions": {"n2b": n2b, "nbc": nbc, "per_body": (n2b + nbc) / n},
-        "phase_ms": {"build": statistics.mean(build_ms), "walk": walk_mean},
+        "ratios": ratios,
+        "headline": {"mode": list(head_mode), "rms": head_err[0], "p99": head_err[1],
+                     "target_rms": target, "guard": guard, "build_ms": head["build_ms"],
+                     "walk_ms": head["walk_ms"], "interactions": head["n2b"] + head["nbc"]},
+        "comparisons": comp,
+        "calibration": {"fixed_theta_0.5": fixed, "error_rule": cal_err, "learned": cal_lrn,
+                        "fixed_theta_1e-3": cal_th, "error_rule_1e-3": cal_err2, "learned_1e-3": cal_lrn2},
+        "training": train,
+        "interactions_per_s": world * (head["n2b"] + head["nbc"]) / (mean_ms * 1e-3),
         "walk_stats": ws,
         "wall_s_timed_loop": wall,
-        "force_error": ferr,
+        "force_error": {"rms": head_err[0], "p99": head_err[1], "sample": int(len(idx)),
+                        "against": "FP64 direct sum (GPU)"},
         "clocks": clocks,
     }
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         pos = np.ascontiguousarray(ph[:, 0])
         v, tb, rate = cpu_leg(n, m, pos, procs=1, nsample_per_proc=args.cpu_sample)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                               "sample": f"oracle port (C, FP64): full tree build of {n} bodies "
-                                         f"({tb:.2f} s) + walks of {args.cpu_sample} sampled bodies "
+                               "sample": f"oracle port (C, FP64) of the fixed-theta walk: full tree build of {n} "
+                                         f"bodies ({tb:.2f} s) + walks of {args.cpu_sample} sampled bodies "
                                          f"({rate:.0f} bodies/s), extrapolated to one full evaluation"}
     ctx.close()
     if rank == 0:

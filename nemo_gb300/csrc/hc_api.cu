@@ -315,6 +315,11 @@ int hc_set_params(hc_ctx *c, const hc_params *p)
         return HC_ERR_ARG;
     }
     c->prm = *p;
+    for (auto &g : static_cast<hc_ctx_ext *>(c)->graphs)   // captured graphs bake tol / eps / usequad
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
     return HC_OK;
 }
 

@@ -51,7 +51,7 @@ struct QueueSmem {
     __nv_bfloat16 x[32 * MLP_XS];     // features of the round's rows
     int node[QCAP];
     unsigned mask[QCAP];
-    float dmin2[QCAP], dmax2[QCAP], p[QCAP];
+    float dmin2[QCAP], dmax2[QCAP], err[QCAP];   // err: the error rule's proxy
     float z[32];                      // the round's logits
 };
 
@@ -62,7 +62,9 @@ struct WarpSmem {
     float4 cl[CCAP];            // cell list: rel pos, mass
     float4 cq0[CCAP];           // Qxx Qxy Qxz Qyy
     float4 cq1[CCAP];           // Qyz Qzz mask(bits) 0
+    unsigned long long stat[8]; // warp totals (lane 0 writes): see the ST_* indices
 };
+enum { ST_N2B, ST_NBC, ST_CAND, ST_MIXED, ST_EB, ST_EC, ST_MLP, ST_ROUNDS };
 
 struct WalkArgs {
     const float4 *nodeA, *nodeB, *nodeQ;
@@ -89,8 +91,7 @@ struct WalkArgs {
     const int *run_flag;                  // when set: the walk runs only if *run_flag != 0
     const MlpSmem *mlp;                   // MODE 3: packed network
     float mlp_threshold;                  // MODE 3: accept iff logit > threshold
-    float band;                           // MODE 3: network band in log2(proxy / budget): [-band, band_hi]
-    float band_hi;
+    float band_lo_f, band_hi_f;           // MODE 3: network band [budget band_lo_f, budget band_hi_f] of the proxy
     int collect;                          // MODE 3: decide analytically, record sampled band candidates
     unsigned keep24;                      // sampling threshold on a 24-bit hash
     int sample_cap;
@@ -239,7 +240,9 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
 //         cell's bodies; p = 3 with quadrupoles, 2 without), is at most
 //         eps_acc times the group's smallest |a| of the previous evaluation.
 template <bool QUAD, bool COUNT, int MODE>
-__global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs g)
+// Register budget: 96 (5 blocks of 4 warps per SM) for the fixed rules; the
+// learned walk's inline network round needs 128 (4 blocks).
+__global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs g)
 {
     if (g.run_flag && *g.run_flag == 0) return;   // guard passed: no fallback walk
     extern __shared__ float4 smem_raw[];
@@ -254,7 +257,9 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
     const int64_t ngroups = ng_table + (g.ntarget - nmassive + 31) / 32;
     const int nnode = g.box->nnode;
     const float tol2 = g.tol2f, eps2 = g.eps2f;
-    unsigned long long tot_b = 0, tot_c = 0, st_cand = 0, st_mixed = 0, st_eb = 0, st_ec = 0, st_mlp = 0, st_rounds = 0;
+    // warp-uniform totals live in shared memory, not in registers
+    if (lane < 8) S.stat[lane] = 0ull;
+    __syncwarp();
     int max_sp = 0, nborder = 0;
 
     while (true) {
@@ -308,9 +313,10 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
         float sphi = 0.f, sax = 0.f, say = 0.f, saz = 0.f;   // Kahan sums
         float cphi = 0.f, cax = 0.f, cay = 0.f, caz = 0.f;
         int myb = 0, myc = 0;                              // per-body counts
+        unsigned gb = 0, gc = 0;                           // this lane's accepted-node interactions
 
         auto flush_bodies = [&](int nb) {
-            st_eb += nb;
+            if (lane == 0) S.stat[ST_EB] += nb;
             float pphi = 0.f, pax = 0.f, pay = 0.f, paz = 0.f;
             for (int e = 0; e < nb; e++) {
                 const float4 P = S.bl[e];
@@ -334,7 +340,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
             kahan_add(saz, caz, paz);
         };
         auto flush_cells = [&](int nc) {
-            st_ec += nc;
+            if (lane == 0) S.stat[ST_EC] += nc;
             float pphi = 0.f, pax = 0.f, pay = 0.f, paz = 0.f;
             for (int e = 0; e < nc; e++) {
                 const float4 P = S.cl[e];
@@ -363,7 +369,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
             unsigned my_mask = 0;
             // MODE 3: a network round decides the first (up to) 32 queued candidates
             const bool mlp_round = MODE == 3 && (qn >= 32 || sp == 0);
-            float logit = 0.f, q_dmin2 = 0.f, q_dmax2 = 0.f, q_p = 0.f;
+            float logit = 0.f, q_dmin2 = 0.f, q_dmax2 = 0.f, q_err = 1.f;
             if (mlp_round) {
                 ncand = qn < 32 ? qn : 32;
                 if (lane < ncand) {
@@ -371,7 +377,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                     my_mask = Qs->mask[lane];
                     q_dmin2 = Qs->dmin2[lane];
                     q_dmax2 = Qs->dmax2[lane];
-                    q_p = Qs->p[lane];
+                    q_err = Qs->err[lane];
                 }
                 __syncwarp();
                 // shift the rest of the queue down
@@ -381,11 +387,13 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                     Qs->mask[lane] = Qs->mask[32 + lane];
                     Qs->dmin2[lane] = Qs->dmin2[32 + lane];
                     Qs->dmax2[lane] = Qs->dmax2[32 + lane];
-                    Qs->p[lane] = Qs->p[32 + lane];
+                    Qs->err[lane] = Qs->err[32 + lane];
                 }
                 qn = rest;
-                st_mlp += ncand;
-                st_rounds++;
+                if (lane == 0) {
+                    S.stat[ST_MLP] += ncand;
+                    S.stat[ST_ROUNDS]++;
+                }
             }
             // ---- gather up to 32 candidates from the top of the stack ----
             while (!mlp_round && ncand < 32 && sp > 0) {
@@ -422,7 +430,8 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                     const float4 Q0 = g.nodeQ[2 * (int64_t)my_node], Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
                     float f[12];
                     cell_features_inl(f, q_dmin2, q_dmax2, B.w, A.w, Q1.w, sqrtf(q_dmin2) - Q1.w, Q0, Q1, amin, rg2,
-                                      eps2, C.y >> 8, (int)cnt, q_p);
+                                      eps2, C.y >> 8, (int)cnt,
+                                      __log2f(fmaxf(q_err, 1e-38f)) - __log2f(g.eps_acc * amin));
 #pragma unroll
                     for (int k = 0; k < 6; k++) w[k] = pack_bf16(f[2 * k], f[2 * k + 1]);
                 }
@@ -438,7 +447,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
             unsigned openm = 0, accm = 0;
             bool mixed = false;
             bool band = false;                 // MODE 3: queued for the network
-            float bd_dmin2 = 0.f, bd_dmax2 = 0.f, bd_p = 0.f;
+            float bd_dmin2 = 0.f, bd_dmax2 = 0.f, bd_err = 0.f;
             if (have) {
                 if (isbody) {
                     const int64_t slot = (int64_t)(-1 - C.x) - s0;     // leaf holds its massive rank
@@ -465,17 +474,18 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                         const float4 Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
                         const float b = Q1.w;
                         const float dmin = sqrtf(dmin2), gap = dmin - b;
-                        float p_raw = 1e30f;
+                        float err = 3.0e38f;           // no expansion (gap <= 0 or size/dmin > 4): open
                         if (gap > 0.f && tmin >= dsq * 0.0625f) {
                             const float gi = 1.f / gap, bg = b * gi;
-                            const float err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
-                            p_raw = __log2f(fmaxf(err, 1e-38f)) - __log2f(g.eps_acc * amin);
+                            err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
                         }
-                        if (p_raw < -g.band) accm = my_mask;
-                        else if (p_raw > g.band_hi) openm = my_mask;
+                        const float budget = g.eps_acc * amin;
+                        if (err < budget * g.band_lo_f) accm = my_mask;          // below the band
+                        else if (err > budget * g.band_hi_f) openm = my_mask;    // above it
                         else if (g.collect) {
                             // label walk: analytic decision, sampled record of the band candidate
-                            if (p_raw <= 0.f) accm = my_mask;
+                            const float p_raw = __log2f(fmaxf(err, 1e-38f)) - __log2f(budget);
+                            if (err <= budget) accm = my_mask;
                             else openm = my_mask;
                             if ((hash2((unsigned)grp, (unsigned)my_node) >> 8) < g.keep24) {
                                 const int slot = atomicAdd(g.sample_count, 1);
@@ -494,7 +504,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                             band = true;
                             bd_dmin2 = dmin2;
                             bd_dmax2 = dmax2;
-                            bd_p = p_raw;
+                            bd_err = err;
                         }
                     } else if (MODE == 2) {
                         const float b = g.nodeQ[2 * (int64_t)my_node + 1].w;
@@ -520,14 +530,16 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                     Qs->mask[row] = my_mask;
                     Qs->dmin2[row] = bd_dmin2;
                     Qs->dmax2[row] = bd_dmax2;
-                    Qs->p[row] = bd_p;
+                    Qs->err[row] = bd_err;
                 }
                 qn += __popc(qb);
                 __syncwarp();
             }
             unsigned mixedb = MODE == 0 ? __ballot_sync(FULL, mixed) : 0u;
-            st_cand += ncand;
-            st_mixed += __popc(mixedb);
+            if (lane == 0) {
+                S.stat[ST_CAND] += ncand;
+                S.stat[ST_MIXED] += __popc(mixedb);
+            }
             while (mixedb) {
                 const int j = __ffs(mixedb) - 1;
                 mixedb &= mixedb - 1;
@@ -580,7 +592,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                 two_diff(A.z, ghz, hz, ez);
                 S.bl[pos] = make_float4(hx, hy, hz, A.w);
                 S.bl2[pos] = make_float4(ex + (B.x - glx), ey + (B.y - gly), ez + (B.z - glz), __uint_as_float(accm));
-                tot_b += __popc(accm);
+                gb += __popc(accm);
             }
             if (ac) {
                 const int pos = nc + __popc(cbal & lt);
@@ -592,7 +604,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
                 } else {
                     S.cq1[pos] = make_float4(0.f, 0.f, __uint_as_float(accm), 0.f);
                 }
-                tot_c += __popc(accm);
+                gc += __popc(accm);
             }
             nb += __popc(bbal);
             nc += __popc(cbal);
@@ -616,6 +628,18 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
         }
         if (nb) flush_bodies(nb);
         if (nc) flush_cells(nc);
+        {
+            unsigned long long sb = gb, sc = gc;           // group totals (up to 32 n: 64-bit)
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+                sb += __shfl_xor_sync(FULL, sb, off);
+                sc += __shfl_xor_sync(FULL, sc, off);
+            }
+            if (lane == 0) {
+                S.stat[ST_N2B] += sb;
+                S.stat[ST_NBC] += sc;
+            }
+        }
         __syncwarp();
 
         if (valid) {
@@ -640,23 +664,20 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 1) k_walk(WalkArgs
     }
     // interaction totals and stats
 #pragma unroll
-    for (int off = 16; off; off >>= 1) {
-        tot_b += __shfl_xor_sync(FULL, tot_b, off);
-        tot_c += __shfl_xor_sync(FULL, tot_c, off);
-        nborder += __shfl_xor_sync(FULL, nborder, off);
-    }
+    for (int off = 16; off; off >>= 1) nborder += __shfl_xor_sync(FULL, nborder, off);
+    __syncwarp();
     if (lane == 0) {
-        atomicAdd(&g.st->n2b, tot_b);
-        atomicAdd(&g.st->nbc, tot_c);
+        atomicAdd(&g.st->n2b, S.stat[ST_N2B]);
+        atomicAdd(&g.st->nbc, S.stat[ST_NBC]);
         atomicMax(&g.st->max_stack, max_sp);
         atomicAdd(&g.st->nborder, nborder);
-        atomicAdd(&g.st->ncand, st_cand);
-        atomicAdd(&g.st->nmixed, st_mixed);
-        atomicAdd(&g.st->nentry_b, st_eb);
-        atomicAdd(&g.st->nentry_c, st_ec);
+        atomicAdd(&g.st->ncand, S.stat[ST_CAND]);
+        atomicAdd(&g.st->nmixed, S.stat[ST_MIXED]);
+        atomicAdd(&g.st->nentry_b, S.stat[ST_EB]);
+        atomicAdd(&g.st->nentry_c, S.stat[ST_EC]);
         if (MODE == 3) {
-            atomicAdd(&g.st->nmlp, st_mlp);
-            atomicAdd(&g.st->nmlp_rounds, st_rounds);
+            atomicAdd(&g.st->nmlp, S.stat[ST_MLP]);
+            atomicAdd(&g.st->nmlp_rounds, S.stat[ST_ROUNDS]);
         }
     }
 }
@@ -754,8 +775,8 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
         a.tol2f = 0.25f;
         a.mlp = c->mlp_packed;
         a.mlp_threshold = c->mlp_threshold;
-        a.band = c->mlp_band;
-        a.band_hi = c->mlp_band_hi;
+        a.band_lo_f = exp2f(-c->mlp_band);
+        a.band_hi_f = exp2f(c->mlp_band_hi);
         a.collect = c->collect;
         a.keep24 = c->keep24;
         a.sample_cap = c->collect_cap;

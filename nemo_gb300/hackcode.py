@@ -205,6 +205,15 @@ class Context:
         raw.argtypes = [_vp, _vp, _vp]
         self._check(raw(self._h, mass_ptr, phase_ptr))
 
+    def set_forces(self, acc=None, phi=None):
+        """Accelerations [n][3] / potentials [n] of a previous evaluation (restart state)."""
+        a = None if acc is None else np.ascontiguousarray(acc, dtype=np.float64).reshape(self.n, 3)
+        p = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64).reshape(self.n)
+        self._check(self._L.hc_set_forces(self._h, _ptr(a), _ptr(p)))
+
+    def set_forces_ptr(self, acc_ptr=None, phi_ptr=None):
+        self._check(self._L.hc_set_forces(self._h, acc_ptr, phi_ptr))
+
     def download_ptr(self, phase_ptr=None, acc_ptr=None, phi_ptr=None):
         """Download to raw host pointers (any may be None)."""
         self._check(self._L.hc_download(self._h, phase_ptr, acc_ptr, phi_ptr))
@@ -343,6 +352,25 @@ class Context:
 
     def learn_band(self, lo: float, hi: float):
         self._check(self._L.hc_learn_set_band(self._h, float(lo), float(hi)))
+
+    def learn_from_self(self, theta: float = 0.03, target: int = 1 << 20, epochs: int = 8, batch: int = 4096,
+                        lr: float = 2e-3, seed: int = 7, band=(1.0, 4.0)) -> dict:
+        """Train the opening network on labels this system generates: with the tree
+        built and accelerations of a previous evaluation on the device, sample
+        about `target` band candidates of the error rule at budget `theta`,
+        label each against a refined walk of its subtree (accept when its
+        relative error is at most the median of the sample), and train on the
+        device.  Leaves the band at its previous value."""
+        self.learn_band(*band)
+        ns = self.learn_collect(theta, target)
+        x, y, rel = self.learn_samples()
+        thr = float(np.median(rel)) if len(rel) else 0.0
+        self.learn_relabel(thr)
+        self.learn_init(seed)
+        loss = self.learn_train(epochs=epochs, batch=batch, lr=lr, seed=seed)
+        z = self.learn_infer(x)
+        acc = float(np.mean((z > 0) == (rel <= thr))) if len(rel) else 0.0
+        return {"samples": int(ns), "label_threshold": thr, "loss": float(loss), "train_accuracy": acc}
 
     def learn_threshold(self, t: float):
         self._check(self._L.hc_learn_set_threshold(self._h, float(t)))
