@@ -429,6 +429,79 @@ def run_ours(args, world, rank, local):
         print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------- ensemble workload
+
+ENS_NSYS, ENS_NMIN, ENS_NMAX, ENS_SEED = 4096, 64, 16384, 1
+ENS_EPS, ENS_DT, ENS_TOL, ENS_DIRECT_MAX = 0.02, 1.0 / 256, 0.6, 1024
+
+
+def ensemble_systems(nsys=ENS_NSYS, seed=ENS_SEED):
+    """Body counts log-uniform in [64, 16384] from a seeded generator; system i
+    is mkplummer(N_i, seed + i)."""
+    rng = np.random.default_rng(seed)
+    return np.rint(np.exp(rng.uniform(np.log(ENS_NMIN), np.log(ENS_NMAX), nsys))).astype(np.int64)
+
+
+def run_ensemble(args, world, rank, local):
+    import torch
+    from nemo_gb300 import build as B
+    B.build()
+    from nemo_gb300 import hackcode as hc
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (the CUDA path has no CPU fallback)")
+    torch.cuda.set_device(local)
+    counts = ensemble_systems(args.nsys)
+    ms, phs = [], []
+    for i, n in enumerate(counts):
+        m, ph = hc.mkplummer(int(n), ENS_SEED + i)
+        ms.append(m)
+        phs.append(ph)
+    m, ph = np.concatenate(ms), np.concatenate(phs)
+    ntot = int(counts.sum())
+    ens = hc.Ensemble(counts, tol=ENS_TOL, eps=ENS_EPS, usequad=False, direct_max=ENS_DIRECT_MAX)
+    ens.upload(m, ph)
+    e0 = ens.step(ENS_DT, 0, energy=True)
+    for k in range(1, args.warmup + 1):
+        ens.step(ENS_DT, k)
+    barrier(world)
+    step_s, tree_ms, direct_ms = [], [], []
+    with ClockSampler(local) as clk:
+        for k in range(args.warmup + 1, args.warmup + 1 + args.steps):
+            t0 = time.perf_counter()
+            e1 = ens.step(ENS_DT, k, energy=(k == args.warmup + args.steps))
+            step_s.append(time.perf_counter() - t0)
+            inf = ens.info()
+            tree_ms.append(inf["tree_ms"])
+            direct_ms.append(inf["direct_ms"])
+    barrier(world)
+    inf = ens.info()
+    mean_ms = reduce_max(1e3 * statistics.mean(step_s), world)
+    value = world * ntot / (mean_ms * 1e-3)
+    drift = np.abs((e1[:, 2] - e0[:, 2]) / e0[:, 2])
+    out = {
+        "metric": "ensemble leapfrog body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: Plummer spheres drawn as mkplummer does (ran3, seed 1 + i)",
+        "config": {"workload": f"ensemble of {len(counts)} Plummer spheres, N log-uniform in "
+                               f"[{ENS_NMIN},{ENS_NMAX}] ({ntot} bodies), eps={ENS_EPS}, dt=1/256; "
+                               f"N<={ENS_DIRECT_MAX}: FP32 direct sum, larger: tree at tol={ENS_TOL}",
+                   "l2": "working set larger than L2 (no flush)", "timing": "host wall clock per step "
+                   "(each step is one CUDA-graph launch followed by a stream synchronisation)"},
+        "gpu_launches": inf["launches"] * args.steps,
+        "phase_ms": {"tree": statistics.mean(tree_ms), "direct": statistics.mean(direct_ms)},
+        "systems": {"tree": inf["nsys_tree"], "direct": inf["nsys_direct"], "bodies_tree": inf["bodies_tree"],
+                    "bodies_direct": inf["bodies_direct"]},
+        "interactions_per_s": (inf["interactions_tree"] + inf["interactions_direct"]) / (mean_ms * 1e-3),
+        "energy_drift": {"median": float(np.median(drift)), "max": float(drift.max()),
+                         "steps": args.warmup + args.steps},
+        "clocks": clk.summary(),
+    }
+    ens.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, world, rank):
@@ -470,10 +543,15 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stats", action="store_true", help="one extra counting walk: mask popcount histogram")
+    ap.add_argument("--workload", default="plummer", choices=["plummer", "ensemble"],
+                    help="plummer: the headline (N=1M); ensemble: 4096 independent systems")
+    ap.add_argument("--nsys", type=int, default=ENS_NSYS)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "ensemble":
+        run_ensemble(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

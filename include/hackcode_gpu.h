@@ -281,6 +281,40 @@ int hc_diagnostics_noalloc(int64_t n, const double *mass, const double *x, const
                            const double *vx, const double *vy, const double *vz, const double *ax,
                            const double *ay, const double *az, const double *phi, double *out36, void *stream);
 
+/* ---- ensembles of independent systems (no counterpart in hackcode1, which
+ * evolves one system per run) ----
+ * nsys systems of counts[s] bodies, stepped together with hackcode1's
+ * leapfrog: systems of more than direct_max bodies share one octree build
+ * (each in its own slot of a forest box, with its own persistent expandbox
+ * root box starting at (-2,-2,-2), 4) and are walked with the per-body rule
+ * at tol; the others use an FP32 direct sum, one thread block per system.
+ * Arrays are the systems' bodies concatenated in the given order. */
+#define HC_ENS_DIRECT_LIMIT 4096
+typedef struct hc_ens hc_ens;
+typedef struct {
+    double tol, eps;
+    int usequad;
+    int direct_max;     /* 0..HC_ENS_DIRECT_LIMIT */
+    double fcells;      /* cell pool of the forest per tree body (0: 1.0) */
+} hc_ens_params;
+typedef struct {
+    int nsys_tree, nsys_direct;
+    int64_t bodies_tree, bodies_direct;
+    int64_t interactions_tree, interactions_direct;   /* of the last step */
+    double tree_ms, direct_ms;                         /* device time of the last step */
+    int64_t launches;                                  /* kernels of one step */
+} hc_ens_stats;
+int hc_ens_create(hc_ens **out, int nsys, const int64_t *counts, const hc_ens_params *params);
+void hc_ens_destroy(hc_ens *e);
+const char *hc_ens_last_error(const hc_ens *e);
+int hc_ens_upload(hc_ens *e, const double *mass, const double *phase);
+/* one step (stepsystem, code.c:159-191): forces with the closing half-kick
+ * when nstep > 0, per-system energies (energy[nsys][3] = KE, PE, total;
+ * may be NULL), then kick-drift.  One CUDA graph per step. */
+int hc_ens_step(hc_ens *e, double dt, int64_t nstep, double *energy);
+int hc_ens_download(hc_ens *e, double *phase, double *acc, double *phi);
+int hc_ens_info(hc_ens *e, hc_ens_stats *out);
+
 #ifdef __cplusplus
 }
 #endif

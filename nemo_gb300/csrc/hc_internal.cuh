@@ -132,6 +132,10 @@ struct hc_ctx {
     int nsample;                          // samples held on the device
     int64_t band_total;                   // band candidates seen by the last collection walk
     int criterion;                        // HC_CRITERION_* of include/hackcode_gpu.h
+    // forest of independent systems (hc_ensemble.cu): the walk of a group
+    // starts at its system's root cell instead of node 0
+    const int32_t *walk_sys_root;         // [system] BFS index of the root cell (-1: none)
+    const int32_t *walk_body_sys;         // [body] system of each body
     // per-evaluation guard of the approximate criteria (hc_guard.cu)
     int64_t guard_n;                      // sampled bodies (0: off)
     double guard_rms_max;

@@ -89,6 +89,7 @@ struct WalkArgs {
     float eps_acc;                        // MODE 2/3 error budget relative to |a|
     const double *pax, *pay, *paz;        // MODE 2/3: accelerations of the previous evaluation
     const int *run_flag;                  // when set: the walk runs only if *run_flag != 0
+    const int32_t *sys_root, *body_sys;   // forest: root cell of each group's system
     const MlpSmem *mlp;                   // MODE 3: packed network
     float mlp_threshold;                  // MODE 3: accept iff logit > threshold
     float band_lo_f, band_hi_f;           // MODE 3: network band [budget band_lo_f, budget band_hi_f] of the proxy
@@ -358,8 +359,16 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
 
         int sp = 0, nb = 0, nc = 0;
         bool overflow = false;
+        int root = 0;
+        if (g.sys_root) {                     // forest: this group's system root
+            root = g.sys_root[g.body_sys[__shfl_sync(FULL, o, 0)]];
+            if (root < 0 || root >= nnode) {
+                if (lane == 0) atomicCAS(&g.st->error, 0, HC_ERR_STATE);
+                continue;
+            }
+        }
         if (nnode > 0) {
-            if (lane == 0) S.stack[0] = make_uint2(0u, vmask);   // root, one node
+            if (lane == 0) S.stack[0] = make_uint2((unsigned)root << 3, vmask);   // root, one node
             sp = 1;
         }
         __syncwarp();
@@ -720,6 +729,8 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     if (ntarget <= 0) return HC_OK;
     WalkArgs a;
     a.run_flag = run_flag;
+    a.sys_root = self ? c->walk_sys_root : nullptr;
+    a.body_sys = c->walk_body_sys;
     a.nodeA = c->nodeA;
     a.nodeB = c->nodeB;
     a.nodeQ = c->nodeQ;

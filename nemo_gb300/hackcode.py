@@ -31,7 +31,9 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_set_graphs", "hc_diagnostics_noalloc", "hc_set_criterion", "hc_set_grouping",
            "hc_learn_nparams", "hc_learn_init", "hc_learn_set_params", "hc_learn_get_params", "hc_learn_infer",
            "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
-           "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band", "hc_set_guard", "hc_guard_stats"]
+           "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band", "hc_set_guard", "hc_guard_stats",
+           "hc_ens_create", "hc_ens_destroy", "hc_ens_last_error", "hc_ens_upload", "hc_ens_step",
+           "hc_ens_download", "hc_ens_info"]
 
 
 class HCError(RuntimeError):
@@ -60,6 +62,18 @@ class WalkStats(C.Structure):
         d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "mask_hist"}
         d["mask_hist"] = [int(x) for x in self.mask_hist]
         return d
+
+
+class EnsParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("eps", C.c_double), ("usequad", C.c_int), ("direct_max", C.c_int),
+                ("fcells", C.c_double)]
+
+
+class EnsStats(C.Structure):
+    _fields_ = [("nsys_tree", C.c_int), ("nsys_direct", C.c_int), ("bodies_tree", C.c_int64),
+                ("bodies_direct", C.c_int64), ("interactions_tree", C.c_int64),
+                ("interactions_direct", C.c_int64), ("tree_ms", C.c_double), ("direct_ms", C.c_double),
+                ("launches", C.c_int64)]
 
 
 class TreeInfo(C.Structure):
@@ -104,6 +118,15 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_set_criterion.argtypes = [_vp, C.c_int, C.c_double]
     L.hc_set_grouping.argtypes = [_vp, C.c_int]
     L.hc_set_guard.argtypes = [_vp, C.c_int64, C.c_double, C.c_uint64]
+    L.hc_ens_create.argtypes = [C.POINTER(_vp), C.c_int, _lp, C.POINTER(EnsParams)]
+    L.hc_ens_destroy.argtypes = [_vp]
+    L.hc_ens_destroy.restype = None
+    L.hc_ens_last_error.argtypes = [_vp]
+    L.hc_ens_last_error.restype = C.c_char_p
+    L.hc_ens_upload.argtypes = [_vp, _dp, _dp]
+    L.hc_ens_step.argtypes = [_vp, C.c_double, C.c_int64, _vp]
+    L.hc_ens_download.argtypes = [_vp, _vp, _vp, _vp]
+    L.hc_ens_info.argtypes = [_vp, C.POINTER(EnsStats)]
     L.hc_guard_stats.argtypes = [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
     L.hc_learn_nparams.argtypes = []
@@ -426,6 +449,64 @@ class Context:
         b, w, n = C.c_double(), C.c_double(), C.c_int64()
         self._check(self._L.hc_last_timing(self._h, C.byref(b), C.byref(w), C.byref(n)))
         return b.value, w.value, n.value
+
+
+class Ensemble:
+    """Independent systems of uneven size stepped together (hc_ens_*): systems of
+    more than direct_max bodies share one forest octree walked with the per-body
+    rule at tol; the others use an FP32 direct sum."""
+
+    def __init__(self, counts, tol=0.6, eps=0.02, usequad=False, direct_max=1024, fcells=1.0):
+        self._L = library()
+        self.counts = np.ascontiguousarray(counts, dtype=np.int64)
+        self.nsys = len(self.counts)
+        self.n = int(self.counts.sum())
+        p = EnsParams(float(tol), float(eps), int(bool(usequad)), int(direct_max), float(fcells))
+        self._h = _vp()
+        r = self._L.hc_ens_create(C.byref(self._h), self.nsys, self.counts, C.byref(p))
+        if r != 0:
+            msg = self._L.hc_ens_last_error(self._h).decode() if self._h.value else ""
+            self.close()
+            raise HCError(r, msg or "hc_ens_create")
+
+    def _check(self, r):
+        if r != 0:
+            raise HCError(r, self._L.hc_ens_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.hc_ens_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, mass, phase):
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        ph = np.ascontiguousarray(phase, dtype=np.float64).reshape(-1, 2, 3)
+        if len(m) != self.n or len(ph) != self.n:
+            raise ValueError("mass/phase length must equal the total body count")
+        self._check(self._L.hc_ens_upload(self._h, m, ph))
+
+    def step(self, dt: float, nstep: int, energy: bool = False):
+        e = np.zeros((self.nsys, 3)) if energy else None
+        self._check(self._L.hc_ens_step(self._h, float(dt), int(nstep), _ptr(e)))
+        return e
+
+    def download(self, phase=True, acc=True, phi=True):
+        ph = np.zeros((self.n, 2, 3)) if phase else None
+        a = np.zeros((self.n, 3)) if acc else None
+        p = np.zeros(self.n) if phi else None
+        self._check(self._L.hc_ens_download(self._h, _ptr(ph), _ptr(a), _ptr(p)))
+        return ph, a, p
+
+    def info(self) -> dict:
+        s = EnsStats()
+        self._check(self._L.hc_ens_info(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
 
 
 # ---------------------------------------------------------------- tool-level calls
