@@ -760,7 +760,7 @@ int hc_set_guard(hc_ctx *ctx, int64_t nsample, double rms_max, uint64_t seed)
     const int slices = hc_guard_slices(c);
     if (slices <= 0) return HC_ERR_CUDA;
     HC_TRY(dalloc(c, &c->guard_idx, nsample));
-    HC_TRY(dalloc(c, &c->guard_part, (int64_t)slices * nsample));
+    HC_TRY(dalloc(c, &c->guard_part, (int64_t)slices * nsample + (nsample + 1) / 2));   // + rel2[nsample] (FP64)
     HC_CUDA(cudaMemcpy(c->guard_idx, pick.data(), sizeof(int64_t) * nsample, cudaMemcpyHostToDevice));
     c->guard_slices = slices;
     c->guard_rms_max = rms_max;

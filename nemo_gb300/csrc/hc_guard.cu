@@ -62,25 +62,44 @@ __global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *ma
     if (valid) part[(int64_t)blockIdx.x * ns + s] = make_float4(ax, ay, az, 0.f);
 }
 
-__global__ void __launch_bounds__(GT) k_guard_check(const float4 *part, int slices, int ns, const int64_t *idx,
-                                                    const double *ax, const double *ay, const double *az,
-                                                    double rms_max, hc_guard_state *gs, hc_status *st)
+// Per sampled body: its direct-sum acceleration (partials summed in slice
+// order, FP64) and its squared relative error.
+__global__ void __launch_bounds__(128) k_guard_rel(const float4 *part, int slices, int ns, const int64_t *idx,
+                                                   const double *ax, const double *ay, const double *az,
+                                                   double *rel2)
+{
+    __shared__ double r[3][128];
+    const int s = blockIdx.x;
+    double dx = 0.0, dy = 0.0, dz = 0.0;
+    for (int b = threadIdx.x; b < slices; b += 128) {
+        const float4 p = part[(int64_t)b * ns + s];
+        dx += (double)p.x;
+        dy += (double)p.y;
+        dz += (double)p.z;
+    }
+    r[0][threadIdx.x] = dx;
+    r[1][threadIdx.x] = dy;
+    r[2][threadIdx.x] = dz;
+    __syncthreads();
+    for (int o = 64; o; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 3; q++) r[q][threadIdx.x] += r[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int64_t i = idx[s];
+        const double ex = ax[i] - r[0][0], ey = ay[i] - r[1][0], ez = az[i] - r[2][0];
+        const double a2 = r[0][0] * r[0][0] + r[1][0] * r[1][0] + r[2][0] * r[2][0];
+        rel2[s] = a2 > 0.0 ? (ex * ex + ey * ey + ez * ez) / a2 : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(GT) k_guard_check(const double *rel2, int ns, double rms_max, hc_guard_state *gs,
+                                                    hc_status *st)
 {
     __shared__ double red[GT];
     double acc = 0.0;
-    for (int s = threadIdx.x; s < ns; s += GT) {
-        double dx = 0.0, dy = 0.0, dz = 0.0;
-        for (int b = 0; b < slices; b++) {
-            const float4 p = part[(int64_t)b * ns + s];
-            dx += (double)p.x;
-            dy += (double)p.y;
-            dz += (double)p.z;
-        }
-        const int64_t i = idx[s];
-        const double ex = ax[i] - dx, ey = ay[i] - dy, ez = az[i] - dz;
-        const double a2 = dx * dx + dy * dy + dz * dz;
-        if (a2 > 0.0) acc += (ex * ex + ey * ey + ez * ez) / a2;
-    }
+    for (int s = threadIdx.x; s < ns; s += GT) acc += rel2[s];
     red[threadIdx.x] = acc;
     __syncthreads();
     for (int o = GT / 2; o; o >>= 1) {
@@ -108,7 +127,7 @@ int hc_guard_slices(hc_ctx *c)
     int dev = 0, nsm = 0;
     HC_CUDA(cudaGetDevice(&dev));
     HC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    return 2 * nsm;
+    return 8 * nsm;
 }
 
 // No CUDA queries here: this runs inside stream capture.
@@ -121,7 +140,8 @@ void hc_guard_launch(hc_ctx *c)
     const dim3 grid((unsigned)slices, (unsigned)((ns + GT - 1) / GT));
     k_guard_direct<<<grid, GT, 0, c->stream>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns,
                                               (float)(c->prm.eps * c->prm.eps), slice, c->guard_part);
-    k_guard_check<<<1, GT, 0, c->stream>>>(c->guard_part, slices, ns, c->guard_idx, c->ax, c->ay, c->az,
-                                           c->guard_rms_max, c->guard, c->st);
-    c->launches += 2;
+    double *rel2 = reinterpret_cast<double *>(c->guard_part + (int64_t)c->guard_slices * ns);
+    k_guard_rel<<<ns, 128, 0, c->stream>>>(c->guard_part, slices, ns, c->guard_idx, c->ax, c->ay, c->az, rel2);
+    k_guard_check<<<1, GT, 0, c->stream>>>(rel2, ns, c->guard_rms_max, c->guard, c->st);
+    c->launches += 3;
 }
