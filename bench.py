@@ -41,11 +41,28 @@ FLOPS_MONO, FLOPS_QUAD = 20, 59          # per interaction, as counted in hc_wal
 L2_FLUSH_BYTES = 512 << 20
 
 
-def workload_config(n, mode=("body", TOL)):
+WORKLOADS = {
+    "plummer": {"n": N_DEFAULT, "seed": SEED, "eps": EPS,
+                "what": "plummer N={n} seed={seed} (mkplummer)"},
+    "hernquist": {"n": 4194304, "seed": 7, "eps": 0.005,
+                  "what": "hernquist N={n} seed={seed} (M=1, a=1, truncated at 100a, Eddington-inverted DF)"},
+}
+
+
+def generate(hc, wl, n):
+    if wl == "hernquist":
+        return hc.mkhernquist(n, WORKLOADS[wl]["seed"], 100.0)
+    return hc.mkplummer(n, WORKLOADS[wl]["seed"])
+
+
+def workload_config(n, mode=("body", TOL), wl="plummer"):
     crit = {"body": "fixed-theta (grav.c subdivp)", "error": "error-bound group rule",
             "learned": "learned opening criterion (guarded)"}[mode[0]]
-    return {"workload": f"plummer N={n} seed={SEED}: one force evaluation (octree build + walk of all bodies)",
-            "n": n, "tol": TOL, "eps": EPS, "usequad": USEQUAD, "criterion": crit, "criterion_setting": list(mode),
+    w = WORKLOADS[wl]
+    what = w["what"].format(n=n, seed=w["seed"])
+    return {"workload": f"{what}: one force evaluation (octree build + walk of all bodies)",
+            "n": n, "tol": TOL, "eps": w["eps"], "usequad": USEQUAD, "criterion": crit,
+            "criterion_setting": list(mode),
             "l2": "flushed between steps (512 MiB write, outside the per-step device timing)",
             "parallelism": "replicas (one independent system per GPU)"}
 
@@ -149,7 +166,7 @@ class ClockSampler:
 # ---------------------------------------------------------------- CPU (oracle) legs
 
 def _cpu_worker(args):
-    path, n, nsample, seed = args
+    path, n, nsample, seed, eps = args
     from oracle import oracle as O
     d = np.load(path)
     m, pos = d["mass"], d["pos"]
@@ -160,12 +177,12 @@ def _cpu_worker(args):
     t1 = time.perf_counter()
     rng = np.random.default_rng(seed)
     idx = rng.choice(n, size=nsample, replace=False)
-    T.forces(TOL, EPS, USEQUAD, test_pos=pos[idx])     # test points: same walk, self not skipped
+    T.forces(TOL, eps, USEQUAD, test_pos=pos[idx])     # test points: same walk, self not skipped
     t2 = time.perf_counter()
     return t1 - t0, t2 - t1, nsample
 
 
-def cpu_leg(n: int, m, pos, procs: int, nsample_per_proc: int, seed: int = 0):
+def cpu_leg(n: int, m, pos, procs: int, nsample_per_proc: int, seed: int = 0, eps: float = EPS):
     """Oracle port timed on host cores: every process builds the full tree
     (the reference's build is serial) and walks its own sample of bodies.
     Returns (bodies/s extrapolated to one full evaluation on `procs` cores,
@@ -179,7 +196,7 @@ def cpu_leg(n: int, m, pos, procs: int, nsample_per_proc: int, seed: int = 0):
     try:
         ctxp = mp.get_context("spawn")
         with ctxp.Pool(procs) as pool:
-            res = pool.map(_cpu_worker, [(path, n, nsample_per_proc, seed + i) for i in range(procs)])
+            res = pool.map(_cpu_worker, [(path, n, nsample_per_proc, seed + i, eps) for i in range(procs)])
     finally:
         os.remove(path)
     t_build = statistics.mean(r[0] for r in res)
@@ -192,17 +209,21 @@ def cpu_leg(n: int, m, pos, procs: int, nsample_per_proc: int, seed: int = 0):
 
 RMS_BUDGET = 1e-3            # the force-error budget of comparison (ii) and of the guard
 GUARD_SAMPLE = 256
-ERROR_EPS = (0.015, 0.02, 0.025, 0.03, 0.035, 0.04, 0.05)
-LEARNED_GRID = ((0.03, -1.0), (0.03, 0.0), (0.04, 0.0), (0.04, 1.0), (0.05, 0.0), (0.05, 1.0), (0.05, 2.0))
-THETA_GRID = (0.56, 0.6, 0.62, 0.64, 0.66, 0.68, 0.7)
-ERROR_EPS_II = (0.4, 0.6, 1.0, 1.5, 2.0, 3.0, 4.0)
-LEARNED_GRID_II = ((0.6, 0.0), (1.0, 0.0), (1.5, 0.0), (2.0, 0.0), (3.0, 0.0), (4.0, 0.0))
+LEARNED_THRESHOLD = 0.0      # logit threshold of the learned criterion (0: the network's own decision)
+BISECT_STEPS = 7
+
+
+TUNING = {"body": None, "group": {"group_max": 32, "list_depth": 64, "grouping": "tree"}}
 
 
 def set_mode(ctx, mode):
     """mode: ("body", theta) | ("error", eps) | ("learned", eps, logit threshold).
     The context's tol is theta for the per-body rule and 0.5 otherwise (the
-    fallback of the guard)."""
+    fallback of the guard).  The per-body rule runs with the autotuner's
+    choice (its interaction sets do not depend on it); the group criteria with
+    32-body tree groups."""
+    t = TUNING["body"] if mode[0] == "body" and TUNING["body"] else TUNING["group"]
+    ctx.set_tuning(t["group_max"], t["list_depth"], t["grouping"])
     if mode[0] == "body":
         ctx.set_params(tol=mode[1])
         ctx.set_criterion("body")
@@ -236,10 +257,25 @@ def point(ctx, mode, idx, ea, reps=3):
     return {"mode": list(mode), "step_ms": min(ts), "rms": rms, "p99": p99, "interactions": int(d.n2b + d.nbc)}
 
 
-def pick(points, target):
-    """Fastest setting whose RMS error is within the target."""
-    ok = [p for p in points if p["rms"] <= target]
-    return min(ok, key=lambda p: p["step_ms"]) if ok else None
+def calibrate(ctx, idx, ea, mode_of, lo, hi, target, geometric=True, steps=BISECT_STEPS):
+    """Largest parameter in [lo, hi] whose RMS error is within the target (RMS
+    grows with the parameter): bisection.  Returns (best point or None, probes)."""
+    probes = [point(ctx, mode_of(hi), idx, ea)]
+    if probes[-1]["rms"] <= target:
+        return probes[-1], probes
+    probes.append(point(ctx, mode_of(lo), idx, ea))
+    if probes[-1]["rms"] > target:
+        return None, probes
+    best = probes[-1]
+    for _ in range(steps):
+        mid = (lo * hi) ** 0.5 if geometric else 0.5 * (lo + hi)
+        pt = point(ctx, mode_of(mid), idx, ea)
+        probes.append(pt)
+        if pt["rms"] <= target:
+            best, lo = pt, mid
+        else:
+            hi = mid
+    return best, probes
 
 
 def timed(ctx, mode, steps, warmup, flush, world):
@@ -282,14 +318,18 @@ def run_ours(args, world, rank, local):
     if not torch.cuda.is_available():
         raise SystemExit("bench.py: no CUDA device (the CUDA path has no CPU fallback)")
     torch.cuda.set_device(local)
-    n = args.n
-    m, ph = hc.mkplummer(n, SEED)
-    ctx = hc.Context(n, tol=TOL, eps=EPS, fcells=1.0, usequad=USEQUAD)
+    wl = args.workload
+    n = args.n if args.n else WORKLOADS[wl]["n"]
+    eps = WORKLOADS[wl]["eps"]
+    m, ph = generate(hc, wl, n)
+    ctx = hc.Context(n, tol=TOL, eps=eps, fcells=1.0, usequad=USEQUAD)
     ctx.upload(m, ph)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         ctx.evaluate()
     peak = ctx.fp32_peak_tflops()
+    tuned = ctx.autotune()                  # per-body rule at tol = 0.5
+    TUNING["body"] = tuned
 
     # ---- FP64 direct-sum sample (bodies do not move: one evaluation per step) ----
     rng = np.random.default_rng(12345)
@@ -308,13 +348,12 @@ def run_ours(args, world, rank, local):
     # ---- calibration to equal RMS (untimed) ----
     fixed = point(ctx, ("body", TOL), idx, ea)
     target = fixed["rms"]
-    cal_err = [point(ctx, ("error", e), idx, ea) for e in ERROR_EPS]
-    cal_lrn = [point(ctx, ("learned", e, t), idx, ea) for e, t in LEARNED_GRID]
-    err_pt, lrn_pt = pick(cal_err, target), pick(cal_lrn, target)
-    cal_th = [point(ctx, ("body", t), idx, ea) for t in THETA_GRID]
-    cal_err2 = [point(ctx, ("error", e), idx, ea) for e in ERROR_EPS_II]
-    cal_lrn2 = [point(ctx, ("learned", e, t), idx, ea) for e, t in LEARNED_GRID_II]
-    th_pt2, err_pt2, lrn_pt2 = pick(cal_th, RMS_BUDGET), pick(cal_err2, RMS_BUDGET), pick(cal_lrn2, RMS_BUDGET)
+    learned_mode = lambda e: ("learned", e, LEARNED_THRESHOLD)
+    err_pt, cal_err = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, target)
+    lrn_pt, cal_lrn = calibrate(ctx, idx, ea, learned_mode, 1e-3, 64.0, target)
+    th_pt2, cal_th = calibrate(ctx, idx, ea, lambda t: ("body", t), TOL, 1.2, RMS_BUDGET, geometric=False)
+    err_pt2, cal_err2 = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, RMS_BUDGET)
+    lrn_pt2, cal_lrn2 = calibrate(ctx, idx, ea, learned_mode, 1e-3, 64.0, RMS_BUDGET)
     head_mode = tuple(lrn_pt["mode"]) if lrn_pt else ("body", TOL)
 
     # ---- timed: the headline (learned, guard on) and its comparisons ----
@@ -393,8 +432,9 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: Plummer sphere drawn as mkplummer does (ran3, seed=1)",
-        "config": workload_config(n, head_mode),
+        "data": ("synthetic: Plummer sphere drawn as mkplummer does (ran3, seed=1)" if wl == "plummer" else
+                 "synthetic: Hernquist sphere (project generator, ran3 seed=7)"),
+        "config": workload_config(n, head_mode, wl),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 80 * n, "d2h_bytes_per_step": 32 * n,
                 "calls": "hc_upload + hc_set_forces (previous accelerations) + hc_evaluate + hc_download"},
         "gpu_launches": head["launches"],
@@ -410,6 +450,7 @@ def run_ours(args, world, rank, local):
         "calibration": {"fixed_theta_0.5": fixed, "error_rule": cal_err, "learned": cal_lrn,
                         "fixed_theta_1e-3": cal_th, "error_rule_1e-3": cal_err2, "learned_1e-3": cal_lrn2},
         "training": train,
+        "tuning": {"fixed_theta": tuned, "group_criteria": TUNING["group"]},
         "interactions_per_s": world * (head["n2b"] + head["nbc"]) / (mean_ms * 1e-3),
         "walk_stats": ws,
         "wall_s_timed_loop": wall,
@@ -419,7 +460,7 @@ def run_ours(args, world, rank, local):
     }
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         pos = np.ascontiguousarray(ph[:, 0])
-        v, tb, rate = cpu_leg(n, m, pos, procs=1, nsample_per_proc=args.cpu_sample)
+        v, tb, rate = cpu_leg(n, m, pos, procs=1, nsample_per_proc=args.cpu_sample, eps=eps)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                                "sample": f"oracle port (C, FP64) of the fixed-theta walk: full tree build of {n} "
                                          f"bodies ({tb:.2f} s) + walks of {args.cpu_sample} sampled bodies "
@@ -509,7 +550,7 @@ def run_reference(args, world, rank):
         return
     from oracle import oracle as O
     O.build(ref=False)
-    n = args.n
+    n = args.n if args.n else N_DEFAULT
     m, ph = O.mkplummer(n, SEED)
     pos = np.ascontiguousarray(ph[:, 0])
     procs = os.cpu_count() or 1
@@ -537,14 +578,15 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--n", type=int, default=0, help="bodies (default: the workload's)")
     ap.add_argument("--sample", type=int, default=16384, help="bodies for the FP64 force-error sample")
     ap.add_argument("--cpu-sample", type=int, default=2048)
     ap.add_argument("--ref-sample", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stats", action="store_true", help="one extra counting walk: mask popcount histogram")
-    ap.add_argument("--workload", default="plummer", choices=["plummer", "ensemble"],
-                    help="plummer: the headline (N=1M); ensemble: 4096 independent systems")
+    ap.add_argument("--workload", default="plummer", choices=["plummer", "hernquist", "ensemble"],
+                    help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
+                         "ensemble: 4096 independent systems")
     ap.add_argument("--nsys", type=int, default=ENS_NSYS)
     args = ap.parse_args()
     world, rank, local = dist_setup()

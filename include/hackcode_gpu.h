@@ -230,6 +230,23 @@ int hc_learn_set_band(hc_ctx *ctx, double lo, double hi);
 enum { HC_GROUPS_CONSECUTIVE = 0, HC_GROUPS_TREE = 1 };
 int hc_set_grouping(hc_ctx *ctx, int kind);
 
+/* Walk tuning (no counterpart in hackcode1): the largest walk group of tree
+ * grouping (1..32 bodies per warp), the interaction-list depth evaluated per
+ * flush (32..64 entries) and the grouping kind.  hc_autotune times one
+ * evaluation of the bodies and criterion currently set for each candidate
+ * (group_max 16/24/32 x list_depth 32/48/64 on tree groups, plus consecutive
+ * groups for the per-body rule), keeps the fastest and returns it with its
+ * time in ms.  With the per-body rule the interaction sets do not depend on
+ * the tuning; with the approximate criteria the group size changes which
+ * cells are accepted. */
+typedef struct {
+    int group_max, list_depth, grouping;
+    double ms;
+} hc_tuning;
+int hc_set_tuning(hc_ctx *ctx, const hc_tuning *t);
+int hc_get_tuning(hc_ctx *ctx, hc_tuning *t);
+int hc_autotune(hc_ctx *ctx, hc_tuning *best);
+
 /* Walk statistics of the last force evaluation: candidates classified,
  * candidates needing the per-body test, interaction-list entries evaluated
  * (bodies, cells; 32 lanes each), borderline decisions re-done in FP64 and the
@@ -257,6 +274,12 @@ int hc_fp32_peak(hc_ctx *ctx, double *tflops);
  * and hackcode1's nbody= test data (hackcode1/code.c:129-153). */
 void hc_mkplummer(int n, int seed, double *mass, double *phase);
 void hc_make_testdata(int n, int seed, int cencon, double *mass, double *phase);
+/* Isotropic Hernquist sphere, G = M = a = 1, truncated at rtrunc (no
+ * counterpart in hackcode1; NEMO's mkhernquist / mkhalo differ): radii from
+ * the truncated mass profile, velocities from the Eddington-inverted
+ * distribution function (Hernquist 1990, eq. 17), equal masses M(rtrunc)/n,
+ * centre of mass at rest at the origin; ran3 seeded with seed. */
+void hc_mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase);
 
 /* Host services of the drop-in programs, exported for tests: copy every
  * snapshot of a filestruct file through the reader and writer (returns the

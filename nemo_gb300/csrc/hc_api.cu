@@ -266,6 +266,8 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
     c->maxnode = nbody + c->maxcell;
     c->mlp_band = 1.0f;
     c->mlp_band_hi = 3.0f;
+    c->group_max = HC_GROUP;
+    c->list_depth = 64;
     *out = c;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         c->err = "cudaStreamCreate failed";
@@ -780,6 +782,70 @@ int hc_guard_stats(hc_ctx *ctx, int64_t *checks, int64_t *trips, double *last_rm
     if (checks) *checks = (int64_t)g.checks;
     if (trips) *trips = (int64_t)g.trips;
     if (last_rms) *last_rms = g.last_rms;
+    return HC_OK;
+}
+
+static void drop_graphs(hc_ctx_ext *c)
+{
+    for (auto &g : c->graphs)
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+}
+
+int hc_set_tuning(hc_ctx *ctx, const hc_tuning *t)
+{
+    if (!ctx || !t) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    if (t->group_max < 1 || t->group_max > HC_GROUP || t->list_depth < 32 || t->list_depth > 64 ||
+        (t->grouping != HC_GROUPS_CONSECUTIVE && t->grouping != HC_GROUPS_TREE)) {
+        c->err = "hc_set_tuning: group_max 1..32, list_depth 32..64, grouping HC_GROUPS_*";
+        return HC_ERR_ARG;
+    }
+    c->group_max = t->group_max;
+    c->list_depth = t->list_depth;
+    c->group_kind = t->grouping;
+    drop_graphs(c);
+    return HC_OK;
+}
+
+int hc_get_tuning(hc_ctx *ctx, hc_tuning *t)
+{
+    if (!ctx || !t) return HC_ERR_ARG;
+    t->group_max = ctx->group_max;
+    t->list_depth = ctx->list_depth;
+    t->grouping = ctx->group_kind;
+    t->ms = 0.0;
+    return HC_OK;
+}
+
+int hc_autotune(hc_ctx *ctx, hc_tuning *best)
+{
+    if (!ctx) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    hc_tuning keep;
+    hc_get_tuning(ctx, &keep);
+    std::vector<hc_tuning> cand;
+    const int gms[] = {16, 24, 32}, lds[] = {32, 48, 64};
+    for (int gm : gms)
+        for (int ld : lds) cand.push_back(hc_tuning{gm, ld, HC_GROUPS_TREE, 0.0});
+    if (c->criterion == HC_CRITERION_BODY)      // the other criteria always walk tree groups
+        for (int ld : lds) cand.push_back(hc_tuning{HC_GROUP, ld, HC_GROUPS_CONSECUTIVE, 0.0});
+    hc_tuning win = keep;
+    win.ms = 1e300;
+    for (hc_tuning &t : cand) {
+        HC_TRY(hc_set_tuning(ctx, &t));
+        double ms = 1e300;
+        for (int rep = 0; rep < 3; rep++) {
+            HC_TRY(run_evaluation(c, 0, 0.0, 0, false));
+            ms = std::min(ms, (double)c->build_ms + (double)c->walk_ms);
+        }
+        t.ms = ms;
+        if (ms < win.ms) win = t;
+    }
+    HC_TRY(hc_set_tuning(ctx, &win));
+    if (best) *best = win;
     return HC_OK;
 }
 

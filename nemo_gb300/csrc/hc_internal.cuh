@@ -132,6 +132,8 @@ struct hc_ctx {
     int nsample;                          // samples held on the device
     int64_t band_total;                   // band candidates seen by the last collection walk
     int criterion;                        // HC_CRITERION_* of include/hackcode_gpu.h
+    int group_max;                        // bodies per tree-aligned walk group (<= HC_GROUP)
+    int list_depth;                       // interaction-list entries evaluated per flush (32..64)
     // forest of independent systems (hc_ensemble.cu): the walk of a group
     // starts at its system's root cell instead of node 0
     const int32_t *walk_sys_root;         // [system] BFS index of the root cell (-1: none)

@@ -571,7 +571,7 @@ __global__ void k_set_nmassive(const int32_t *total, hc_box *box) { box->nmassiv
 
 // ---------------- walk groups aligned with the tree ----------------
 // A group is a run of massive bodies (in key order) that lie in one cell of
-// at most HC_GROUP bodies: the cells (and lone bodies) with <= HC_GROUP bodies
+// at most gmax (<= HC_GROUP) bodies: the cells (and lone bodies) with <= gmax bodies
 // whose parent has more, consecutive siblings packed while they fit.
 
 __device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t *pre_a, const int32_t *pre_b, int k,
@@ -589,8 +589,8 @@ __device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t
 
 template <bool EMIT>
 __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const int32_t *pre_b, const int32_t *parent,
-                         const int2 *nodeC, const hc_box *box, int64_t maxnode, int32_t *ng, const int32_t *goff,
-                         int32_t *gstart, int32_t *gcount)
+                         const int2 *nodeC, const hc_box *box, int64_t maxnode, int gmax, int32_t *ng,
+                         const int32_t *goff, int32_t *gstart, int32_t *gcount)
 {
     const int nn = box->nnode;
     for (int64_t kk = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; kk < maxnode;
@@ -603,7 +603,7 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const in
         int first;
         const int cnt = node_count(bfs2pre, pre_a, pre_b, k, &first);
         int out = EMIT ? goff[k] : 0, packs = 0;
-        if (cnt <= HC_GROUP) {                     // only the root can be a small group on its own here
+        if (cnt <= gmax) {                         // only the root can be a small group on its own here
             if (parent[k] < 0) {
                 if (EMIT) {
                     gstart[out] = first;
@@ -617,7 +617,7 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const in
             for (int i = 0; i < nc; i++) {
                 int f;
                 const int cc = node_count(bfs2pre, pre_a, pre_b, fc + i, &f);
-                if (cc > HC_GROUP || cur + cc > HC_GROUP) {
+                if (cc > gmax || cur + cc > gmax) {
                     if (cur > 0) {
                         if (EMIT) {
                             gstart[out + packs] = cur_first;
@@ -626,7 +626,7 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const in
                         packs++;
                         cur = 0;
                     }
-                    if (cc > HC_GROUP) continue;
+                    if (cc > gmax) continue;
                 }
                 if (cur == 0) cur_first = f;
                 cur += cc;
@@ -736,12 +736,13 @@ int hc_tree_build(hc_ctx *c)
     }
 
     // 7. walk groups aligned with the tree
+    const int gmax = c->group_max >= 1 && c->group_max <= HC_GROUP ? c->group_max : HC_GROUP;
     k_groups<false><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->pre_b, c->parent, c->nodeC,
-                                     c->box, c->maxnode, c->gcnt, nullptr, nullptr, nullptr);
+                                     c->box, c->maxnode, gmax, c->gcnt, nullptr, nullptr, nullptr);
     hc_scan_exclusive_i32(c, c->gcnt, c->goff, c->maxnode + 1, nullptr);
     k_set_ngroups<<<1, 1, 0, s>>>(c->goff, c->maxnode, c->box);
     k_groups<true><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->pre_b, c->parent, c->nodeC, c->box, c->maxnode,
-                                    nullptr, c->goff, c->gstart, c->gcount);
+                                    gmax, nullptr, c->goff, c->gstart, c->gcount);
     c->launches += 3;
     return HC_OK;
 }

@@ -89,6 +89,7 @@ struct WalkArgs {
     float eps_acc;                        // MODE 2/3 error budget relative to |a|
     const double *pax, *pay, *paz;        // MODE 2/3: accelerations of the previous evaluation
     const int *run_flag;                  // when set: the walk runs only if *run_flag != 0
+    int flush_at;                         // lists are evaluated once they hold more entries (<= 32)
     const int32_t *sys_root, *body_sys;   // forest: root cell of each group's system
     const MlpSmem *mlp;                   // MODE 3: packed network
     float mlp_threshold;                  // MODE 3: accept iff logit > threshold
@@ -618,11 +619,11 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
             nb += __popc(bbal);
             nc += __popc(cbal);
             __syncwarp();
-            if (nb > BCAP - 32) {
+            if (nb > g.flush_at) {
                 flush_bodies(nb);
                 nb = 0;
             }
-            if (nc > CCAP - 32) {
+            if (nc > g.flush_at) {
                 flush_cells(nc);
                 nc = 0;
             }
@@ -729,6 +730,10 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     if (ntarget <= 0) return HC_OK;
     WalkArgs a;
     a.run_flag = run_flag;
+    {
+        const int depth = c->list_depth >= 32 && c->list_depth <= BCAP ? c->list_depth : BCAP;
+        a.flush_at = depth - 32;          // an iteration appends at most 32 entries
+    }
     a.sys_root = self ? c->walk_sys_root : nullptr;
     a.body_sys = c->walk_body_sys;
     a.nodeA = c->nodeA;

@@ -162,6 +162,108 @@ void mkplummer(int n, int seed, double *mass, double *phase)
         }
 }
 
+// ---------------------------------------------------------------- Hernquist sphere
+//
+// Model (Hernquist 1990, ApJ 356, 359), G = M = a = 1:
+//   cumulative mass M(r) = r^2 / (1 + r)^2, relative potential psi(r) = 1 / (1 + r),
+//   isotropic distribution function of the relative energy E (eq. 17), q = sqrt(E):
+//   f(E) = [3 asin q + q sqrt(1 - q^2) (1 - 2 q^2) (8 q^4 - 8 q^2 - 3)]
+//          / (8 sqrt(2) pi^3 (1 - q^2)^(5/2)).
+// Radii are drawn from M(r) truncated at rtrunc; at radius r the speed has
+// density g(v) = v^2 f(psi - v^2 / 2) on [0, sqrt(2 psi)) and is drawn by
+// rejection under a tabulated bound of max g (the untruncated potential is
+// used for the velocities).  Every body has mass M(rtrunc) / n.  The centre
+// of mass and its velocity are removed at the end.
+
+static double hernquist_df(double E)
+{
+    const double pi = 3.141592653589793238462643;
+    if (!(E > 0.0)) return 0.0;
+    if (E >= 1.0) E = 1.0 - 1e-15;
+    const double q = std::sqrt(E), q2 = E, s = 1.0 - q2;
+    const double num = 3.0 * std::asin(q) + q * std::sqrt(s) * (1.0 - 2.0 * q2) * (8.0 * q2 * q2 - 8.0 * q2 - 3.0);
+    return num / (8.0 * std::sqrt(2.0) * pi * pi * pi * std::pow(s, 2.5));
+}
+
+// max over v of v^2 f(psi - v^2/2): grid on v = vmax t^2 (fine near 0, where
+// the peak sits for psi near 1), then golden-section refinement
+static double hernquist_gmax(double psi)
+{
+    const double vmax = std::sqrt(2.0 * psi);
+    auto g = [psi](double v) { return v * v * hernquist_df(psi - 0.5 * v * v); };
+    const int K = 96;
+    int kbest = 0;
+    double best = -1.0;
+    for (int k = 1; k < K; k++) {
+        const double t = (double)k / K, v = vmax * t * t;
+        const double y = g(v);
+        if (y > best) {
+            best = y;
+            kbest = k;
+        }
+    }
+    double lo = vmax * std::pow((double)(kbest - 1) / K, 2.0), hi = vmax * std::pow((double)(kbest + 1) / K, 2.0);
+    const double gr = 0.6180339887498949;
+    for (int it = 0; it < 40; it++) {
+        const double a = hi - gr * (hi - lo), b = lo + gr * (hi - lo);
+        if (g(a) > g(b)) hi = b;
+        else lo = a;
+    }
+    return std::max(best, g(0.5 * (lo + hi)));
+}
+
+void mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase)
+{
+    const double two_pi = 6.283185307179586476925287;
+    Ran3 r(seed);
+    const double mt = rtrunc * rtrunc / ((1.0 + rtrunc) * (1.0 + rtrunc));
+    // bound table on log-spaced radii: gmax is smooth in r; use the larger
+    // neighbour and a 10% margin
+    const int T = 2048;
+    const double lr0 = std::log(1e-7), lr1 = std::log(rtrunc * 1.01);
+    std::vector<double> tab(T);
+    for (int k = 0; k < T; k++) tab[k] = hernquist_gmax(1.0 / (1.0 + std::exp(lr0 + (lr1 - lr0) * k / (T - 1))));
+    for (int i = 0; i < n; i++) {
+        double *p = phase + 6 * i, *v = p + 3;
+        mass[i] = mt / (double)n;
+        const double u = std::sqrt(r.uniform(0.0, mt));
+        const double radius = u / (1.0 - u);
+        double theta = std::acos(r.uniform(-1.0, 1.0));
+        double phi = r.uniform(0.0, two_pi);
+        p[0] = radius * std::sin(theta) * std::cos(phi);
+        p[1] = radius * std::sin(theta) * std::sin(phi);
+        p[2] = radius * std::cos(theta);
+        const double psi = 1.0 / (1.0 + radius), vesc = std::sqrt(2.0 * psi);
+        double x = (std::log(std::max(radius, 1e-7)) - lr0) / (lr1 - lr0) * (T - 1);
+        int k = (int)x;
+        if (k < 0) k = 0;
+        if (k > T - 2) k = T - 2;
+        const double bound = 1.1 * std::max(tab[k], tab[k + 1]);
+        double speed;
+        for (;;) {
+            speed = r.uniform(0.0, vesc);
+            const double y = r.uniform(0.0, bound);
+            if (y <= speed * speed * hernquist_df(psi - 0.5 * speed * speed)) break;
+        }
+        theta = std::acos(r.uniform(-1.0, 1.0));
+        phi = r.uniform(0.0, two_pi);
+        v[0] = speed * std::sin(theta) * std::cos(phi);
+        v[1] = speed * std::sin(theta) * std::sin(phi);
+        v[2] = speed * std::cos(theta);
+    }
+    double wp[3] = {0, 0, 0}, wv[3] = {0, 0, 0};
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++) {
+            wp[k] += phase[6 * i + k];
+            wv[k] += phase[6 * i + 3 + k];
+        }
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++) {
+            phase[6 * i + k] -= wp[k] / n;
+            phase[6 * i + 3 + k] -= wv[k] / n;
+        }
+}
+
 // ---------------------------------------------------------------- filestruct
 
 static const short SING_MAGIC = (011 << 8) + 0222, PLUR_MAGIC = (013 << 8) + 0222;  // filesecret.h:26-27
@@ -685,6 +787,10 @@ double hc_nemo_eval(const char *expr, int *ok)
 }
 
 void hc_mkplummer(int n, int seed, double *mass, double *phase) { nemo::mkplummer(n, seed, mass, phase); }
+void hc_mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase)
+{
+    nemo::mkhernquist(n, seed, rtrunc, mass, phase);
+}
 void hc_make_testdata(int n, int seed, int cencon, double *mass, double *phase)
 {
     nemo::make_testdata(n, seed, cencon != 0, mass, phase);

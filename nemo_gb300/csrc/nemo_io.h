@@ -26,6 +26,9 @@ private:
 void make_testdata(int n, int seed, bool cencon, double *mass, double *phase);
 // mkplummer with its defaults (src/nbody/init/mkplummer.c:257-422)
 void mkplummer(int n, int seed, double *mass, double *phase);
+// isotropic Hernquist sphere (G = M = a = 1) truncated at rtrunc; velocities
+// from the Eddington-inverted distribution function (project-written)
+void mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase);
 
 // ---- filestruct (src/kernel/io/filesecret.c, inc/filestruct.h)
 struct Item {

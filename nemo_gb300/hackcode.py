@@ -26,14 +26,14 @@ ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "cell pool exhausted", -4: "
 EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_upload", "hc_set_box", "hc_get_box",
            "hc_build_tree", "hc_tree_summary", "hc_dump_tree", "hc_forces", "hc_forces_at", "hc_download",
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
-           "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_make_testdata",
+           "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_mkhernquist", "hc_make_testdata",
            "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate",
            "hc_set_graphs", "hc_diagnostics_noalloc", "hc_set_criterion", "hc_set_grouping",
            "hc_learn_nparams", "hc_learn_init", "hc_learn_set_params", "hc_learn_get_params", "hc_learn_infer",
            "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
            "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band", "hc_set_guard", "hc_guard_stats",
            "hc_ens_create", "hc_ens_destroy", "hc_ens_last_error", "hc_ens_upload", "hc_ens_step",
-           "hc_ens_download", "hc_ens_info"]
+           "hc_ens_download", "hc_ens_info", "hc_set_tuning", "hc_get_tuning", "hc_autotune"]
 
 
 class HCError(RuntimeError):
@@ -62,6 +62,14 @@ class WalkStats(C.Structure):
         d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "mask_hist"}
         d["mask_hist"] = [int(x) for x in self.mask_hist]
         return d
+
+
+class Tuning(C.Structure):
+    _fields_ = [("group_max", C.c_int), ("list_depth", C.c_int), ("grouping", C.c_int), ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {"group_max": self.group_max, "list_depth": self.list_depth,
+                "grouping": ["consecutive", "tree"][self.grouping], "ms": self.ms}
 
 
 class EnsParams(C.Structure):
@@ -118,6 +126,9 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_set_criterion.argtypes = [_vp, C.c_int, C.c_double]
     L.hc_set_grouping.argtypes = [_vp, C.c_int]
     L.hc_set_guard.argtypes = [_vp, C.c_int64, C.c_double, C.c_uint64]
+    L.hc_set_tuning.argtypes = [_vp, C.POINTER(Tuning)]
+    L.hc_get_tuning.argtypes = [_vp, C.POINTER(Tuning)]
+    L.hc_autotune.argtypes = [_vp, C.POINTER(Tuning)]
     L.hc_ens_create.argtypes = [C.POINTER(_vp), C.c_int, _lp, C.POINTER(EnsParams)]
     L.hc_ens_destroy.argtypes = [_vp]
     L.hc_ens_destroy.restype = None
@@ -157,6 +168,8 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_fp32_peak.argtypes = [_vp, C.POINTER(C.c_double)]
     L.hc_mkplummer.argtypes = [C.c_int, C.c_int, _dp, _dp]
     L.hc_mkplummer.restype = None
+    L.hc_mkhernquist.argtypes = [C.c_int, C.c_int, C.c_double, _dp, _dp]
+    L.hc_mkhernquist.restype = None
     L.hc_make_testdata.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
     L.hc_make_testdata.restype = None
     L.hc_snapcopy.argtypes = [C.c_char_p, C.c_char_p]
@@ -300,6 +313,21 @@ class Context:
     def set_grouping(self, kind: str = "consecutive"):
         """Walk groups: 'consecutive' (32 bodies in key order) or 'tree' (cells of <= 32 bodies)."""
         self._check(self._L.hc_set_grouping(self._h, {"consecutive": 0, "tree": 1}[kind]))
+
+    def set_tuning(self, group_max=32, list_depth=64, grouping="consecutive"):
+        t = Tuning(int(group_max), int(list_depth), {"consecutive": 0, "tree": 1}[grouping], 0.0)
+        self._check(self._L.hc_set_tuning(self._h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        self._check(self._L.hc_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def autotune(self) -> dict:
+        """Time one evaluation per candidate tuning and keep the fastest."""
+        t = Tuning()
+        self._check(self._L.hc_autotune(self._h, C.byref(t)))
+        return t.as_dict()
 
     def set_guard(self, nsample: int, rms_max: float = 1e-3, seed: int = 1):
         """Per-evaluation guard of the approximate criteria (0 samples: off)."""
@@ -516,6 +544,15 @@ def mkplummer(n: int, seed: int = 0):
     m = np.zeros(n)
     ph = np.zeros((n, 2, 3))
     library().hc_mkplummer(int(n), int(seed), m, ph)
+    return m, ph
+
+
+def mkhernquist(n: int, seed: int = 7, rtrunc: float = 100.0):
+    """Isotropic Hernquist sphere (G = M = a = 1, truncated at rtrunc, velocities from
+    the Eddington-inverted distribution function): (mass[n], phase[n,2,3])."""
+    m = np.zeros(n)
+    ph = np.zeros((n, 2, 3))
+    library().hc_mkhernquist(int(n), int(seed), float(rtrunc), m, ph)
     return m, ph
 
 

@@ -161,3 +161,29 @@ def test_keyword_expression_errors(lib):
     ok = C.c_int()
     lib.library().hc_nemo_eval(b"1/", C.byref(ok))
     assert ok.value == 0
+
+
+def test_mkhernquist_moments():
+    """The Hernquist generator (no reference counterpart, parity unpinned):
+    radii follow the truncated mass profile, kinetic energy and isotropy
+    match the model's distribution function."""
+    from nemo_gb300 import hackcode as hc
+    n = 100000
+    m, ph = hc.mkhernquist(n, 7, 100.0)
+    m2, ph2 = hc.mkhernquist(n, 7, 100.0)
+    np.testing.assert_array_equal(ph, ph2)                      # deterministic for a seed
+    mt = 100.0 ** 2 / 101.0 ** 2
+    np.testing.assert_allclose(m.sum(), mt, rtol=1e-12)
+    assert np.abs(ph[:, 0].mean(0)).max() < 1e-12 and np.abs(ph[:, 1].mean(0)).max() < 1e-12
+    r = np.sort(np.linalg.norm(ph[:, 0], axis=1))
+    cdf = (r / (1 + r)) ** 2 / mt
+    ks = np.max(np.abs(np.arange(1, n + 1) / n - cdf))
+    assert ks < 1.63 / np.sqrt(n), ks                            # 1% level
+    v = ph[:, 1]
+    ke = 0.5 * np.sum(m * (v ** 2).sum(1))
+    assert abs(ke - 1.0 / 12.0) < 0.02 / 12.0, ke               # 2K = |W| = 1/6 for the model
+    x = ph[:, 0]
+    rr = np.linalg.norm(x, axis=1)
+    vr2 = np.mean((np.sum(x * v, 1) / rr) ** 2)
+    vt2 = np.mean((v ** 2).sum(1)) - vr2
+    assert abs(vt2 / (2 * vr2) - 1.0) < 0.02, vt2 / (2 * vr2)   # isotropic
