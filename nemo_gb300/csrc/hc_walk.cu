@@ -214,23 +214,25 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
     const float rinv2 = rinv * rinv;
     const float mr = on ? P.w * rinv : 0.f;
     const float mr3 = mr * rinv2;
-    pphi -= mr;
-    pax = fmaf(mr3, dx, pax);
-    pay = fmaf(mr3, dy, pay);
-    paz = fmaf(mr3, dz, paz);
-    if (QUAD) {
-        const float qx = fmaf(Q0.x, dx, fmaf(Q0.y, dy, Q0.z * dz));
-        const float qy = fmaf(Q0.y, dx, fmaf(Q0.w, dy, qyz * dz));
-        const float qz = fmaf(Q0.z, dx, fmaf(qyz, dy, qzz * dz));
-        const float dqd = fmaf(qx, dx, fmaf(qy, dy, qz * dz));
-        const float r5 = on ? rinv2 * rinv2 * rinv : 0.f;
-        const float t = dqd * r5;                 // dr.Q.dr / r^5
-        pphi = fmaf(-0.5f, t, pphi);              // phiquad = -t/2
-        const float sq = 2.5f * t * rinv2;        // -5 phiquad / r^2
-        pax = fmaf(sq, dx, fmaf(-r5, qx, pax));
-        pay = fmaf(sq, dy, fmaf(-r5, qy, pay));
-        paz = fmaf(sq, dz, fmaf(-r5, qz, paz));
+    if (!QUAD) {
+        pphi -= mr;
+        pax = fmaf(mr3, dx, pax);
+        pay = fmaf(mr3, dy, pay);
+        paz = fmaf(mr3, dz, paz);
+        return;
     }
+    const float qx = fmaf(Q0.x, dx, fmaf(Q0.y, dy, Q0.z * dz));
+    const float qy = fmaf(Q0.y, dx, fmaf(Q0.w, dy, qyz * dz));
+    const float qz = fmaf(Q0.z, dx, fmaf(qyz, dy, qzz * dz));
+    const float dqd = fmaf(qx, dx, fmaf(qy, dy, qz * dz));
+    const float r5 = (on ? rinv2 : 0.f) * (rinv2 * rinv);
+    const float t = dqd * r5;                 // dr.Q.dr / r^5
+    pphi -= fmaf(0.5f, t, mr);                // phi: -m/r - t/2
+    // a = dr (m/r^3 + 5/2 t/r^2) - Q.dr / r^5: one coefficient on dr
+    const float c = fmaf(2.5f * rinv2, t, mr3);
+    pax = fmaf(c, dx, fmaf(-r5, qx, pax));
+    pay = fmaf(c, dy, fmaf(-r5, qy, pay));
+    paz = fmaf(c, dz, fmaf(-r5, qz, paz));
 }
 
 // MODE 0: the reference's per-body opening rule (exact interaction sets).
@@ -344,10 +346,13 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
         auto flush_cells = [&](int nc) {
             if (lane == 0) S.stat[ST_EC] += nc;
             float pphi = 0.f, pax = 0.f, pay = 0.f, paz = 0.f;
+            // group criteria accept a cell for the whole group (a cell holding
+            // the group's own bodies is always opened): no per-lane mask test
+            constexpr bool MASKED = MODE == 0 || COUNT;
             for (int e = 0; e < nc; e++) {
                 const float4 P = S.cl[e];
-                const float4 Q1 = S.cq1[e];
-                const bool bit = (__float_as_uint(Q1.z) >> lane) & 1u;
+                const float4 Q1 = (QUAD || MASKED) ? S.cq1[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const bool bit = MASKED ? ((__float_as_uint(Q1.z) >> lane) & 1u) : true;
                 const float4 Q0 = QUAD ? S.cq0[e] : make_float4(0.f, 0.f, 0.f, 0.f);
                 cell_term<QUAD>(P, Q0, Q1.x, Q1.y, bit, bx, by, bz, eps2, pphi, pax, pay, paz);
                 if (COUNT) myc += bit;
