@@ -174,7 +174,16 @@ int hc_last_timing(hc_ctx *ctx, double *build_ms, double *walk_ms, int64_t *laun
  *     theta * |a| are decided by the trained network (hc_learn_*), accepted
  *     when its logit exceeds the threshold of hc_learn_set_threshold.  No
  *     counterpart in hackcode1. */
-enum { HC_CRITERION_BODY = 0, HC_CRITERION_GROUP = 1, HC_CRITERION_ERROR = 2, HC_CRITERION_LEARNED = 3 };
+/* HC_CRITERION_BH86, _SW94, _BARNES: treecode1's critical radii (setrcrit,
+ *     treecode1/treeload.c:232-252: (size/theta)^2; (largest distance from
+ *     the centre of mass to a cell corner / theta)^2; the default
+ *     (size/theta + |cm - cell centre|)^2) in a group walk: a cell is
+ *     accepted for the group iff the squared distance from the group's
+ *     bounding box to its centre of mass exceeds the critical radius
+ *     (treecode1/treegrav.c:137-157 tests the box of the target cell, and
+ *     adds an adjacency test a bounding box does not need). */
+enum { HC_CRITERION_BODY = 0, HC_CRITERION_GROUP = 1, HC_CRITERION_ERROR = 2, HC_CRITERION_LEARNED = 3,
+       HC_CRITERION_BH86 = 4, HC_CRITERION_SW94 = 5, HC_CRITERION_BARNES = 6 };
 int hc_set_criterion(hc_ctx *ctx, int criterion, double theta);
 
 /* Guard of the group, error and learned criteria (no counterpart in

@@ -74,7 +74,8 @@ void free_all(hc_ctx *c)
         if (p) cudaFree(p);
     void *mptrs[] = {c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_grad, c->mlp_loss, c->mlp_gpart, c->mlp_lpart,
                      c->mlp_packed, c->sample_count, c->sample_x, c->sample_amin, c->sample_y, c->sample_rel,
-                     c->sample_w, c->sample_group, c->sample_node, c->guard_idx, c->guard_part, c->guard};
+                     c->sample_w, c->sample_group, c->sample_node, c->guard_idx, c->guard_part, c->guard,
+                     c->rcrit2};
     for (void *p : mptrs)
         if (p) cudaFree(p);
     if (c->h_st) cudaFreeHost(c->h_st);
@@ -557,6 +558,7 @@ static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bo
     HC_CUDA(cudaMemsetAsync(c->st, 0, sizeof(hc_status), c->stream));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[0], c->stream, rflags));
     HC_TRY(hc_tree_build(c));
+    if (c->criterion >= HC_CRITERION_BH86) hc_rcrit_launch(c, c->criterion - HC_CRITERION_BH86 + 1, c->group_theta);
     HC_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, rflags));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, rflags));
     HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
@@ -700,9 +702,10 @@ int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t ns, double *acc,
 
 int hc_set_criterion(hc_ctx *ctx, int criterion, double theta)
 {
-    if (!ctx || criterion < HC_CRITERION_BODY || criterion > HC_CRITERION_LEARNED) return HC_ERR_ARG;
+    if (!ctx || criterion < HC_CRITERION_BODY || criterion > HC_CRITERION_BARNES) return HC_ERR_ARG;
     if (criterion != HC_CRITERION_BODY && !(theta >= 0.0)) return HC_ERR_ARG;
     hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    if (criterion >= HC_CRITERION_BH86 && !c->rcrit2) HC_TRY(dalloc(c, &c->rcrit2, c->maxnode));
     c->criterion = criterion;
     c->group_theta = theta;
     for (auto &g : c->graphs)        // captured graphs bake the walk variant

@@ -508,13 +508,15 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             cz = ddiv(cz, m);
             // bmax: radius around the centre of mass holding every body of the
             // cell (children's extents shifted to the new centre)
-            float bmax = 0.f;
+            float bmax = 0.f, nbody = 0.f;
             for (int i = 0; i < nc; i++) {
                 const int ch = fc + i;
                 const float dx = __double2float_rn(dsub(ncx[ch], cx)), dy = __double2float_rn(dsub(ncy[ch], cy)),
                             dz = __double2float_rn(dsub(ncz[ch], cz));
-                const float bc = nodeC[ch].x >= 0 ? nodeQ[2 * (int64_t)ch + 1].w : 0.f;
-                bmax = fmaxf(bmax, sqrtf(dx * dx + dy * dy + dz * dz) + bc);
+                const bool cell = nodeC[ch].x >= 0;
+                const float4 q1 = cell ? nodeQ[2 * (int64_t)ch + 1] : make_float4(0.f, 0.f, 1.f, 0.f);
+                bmax = fmaxf(bmax, sqrtf(dx * dx + dy * dy + dz * dz) + q1.w);
+                nbody += q1.z;                   // bodies in the cell (exact below 2^24)
             }
             // Q = sum_child [ m (3 dr dr^T - |dr|^2 I) + Q_child ], dr = x_child - x_cm
             float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -551,7 +553,7 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             nodeA[k] = A;
             nodeB[k] = B;
             nodeQ[2 * (int64_t)k] = make_float4(Q[0], Q[1], Q[2], Q[3]);
-            nodeQ[2 * (int64_t)k + 1] = make_float4(Q[4], Q[5], 0.f, bmax);
+            nodeQ[2 * (int64_t)k + 1] = make_float4(Q[4], Q[5], nbody, bmax);
         }
         grid.sync();
     }
@@ -645,7 +647,59 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const in
 
 __global__ void k_set_ngroups(const int32_t *goff, int64_t maxnode, hc_box *box) { box->ngroups = goff[maxnode]; }
 
+// ---------------- treecode1 critical radii ----------------
+// setrcrit (treecode1/treeload.c:232-252) for every cell: the cell's centre
+// and size follow from the integer coordinate of its first body at the
+// cell's depth; cm is the FP64 centre of mass.
+//   bh86: (size/theta)^2;  sw94: (max distance from cm to a corner)^2/theta^2;
+//   "new" (treecode1's default): (size/theta + |cm - centre|)^2;
+//   theta = 0: (2 rsize)^2 (always open).
+__global__ void k_rcrit(int kind, double theta, const hc_box *box, const uint32_t *bfs2pre, const int32_t *pre_a,
+                        const uint32_t *midx, const double *px, const double *py, const double *pz, const int2 *nodeC,
+                        const double *ncx, const double *ncy, const double *ncz, float *rcrit2)
+{
+    const int nn = box->nnode;
+    const double rsize = box->rsize;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+        const int2 C = nodeC[k];
+        if (C.x < 0) continue;                           // body leaf
+        const int D = C.y >> 8;
+        const uint32_t o = midx[pre_a[bfs2pre[k]]];
+        const double p[3] = {px[o], py[o], pz[o]}, cm[3] = {ncx[k], ncy[k], ncz[k]};
+        const double size = ldexp(rsize, -D), unit = ldexp(rsize, -30);
+        const int shift = 30 - D;
+        double off2 = 0.0, bmax2 = 0.0;
+        for (int d = 0; d < 3; d++) {
+            int xi = 0;
+            intcoord1(p[d], box->rmin[d], rsize, &xi);
+            const double corner = box->rmin[d] + (double)((xi >> shift) << shift) * unit;
+            const double dk = cm[d] - (corner + 0.5 * size);       // offset of cm from the centre
+            off2 += dk * dk;
+            const double dc = dk + 0.5 * size;                      // distance from the low corner
+            const double m = dc > size - dc ? dc : size - dc;
+            bmax2 += m * m;
+        }
+        double r2;
+        if (theta == 0.0) r2 = 4.0 * rsize * rsize;
+        else if (kind == 1) r2 = (size / theta) * (size / theta);
+        else if (kind == 2) r2 = bmax2 / (theta * theta);
+        else {
+            const double r = size / theta + sqrt(off2);
+            r2 = r * r;
+        }
+        rcrit2[k] = (float)r2;
+    }
+}
+
 }  // namespace
+
+void hc_rcrit_launch(hc_ctx *c, int kind, double theta)
+{
+    k_rcrit<<<hc_grid(c->maxnode, 256), 256, 0, c->stream>>>(kind, theta, c->box, c->bfs2pre, c->pre_a, c->midx,
+                                                              c->px, c->py, c->pz, c->nodeC, c->ncx, c->ncy, c->ncz,
+                                                              c->rcrit2);
+    c->launches++;
+}
 
 void hc_keys_for_points(hc_ctx *c, const double *x, const double *y, const double *z, int64_t n,
                         unsigned long long *khi, uint32_t *klo, uint32_t *kval)

@@ -90,6 +90,7 @@ struct WalkArgs {
     const double *pax, *pay, *paz;        // MODE 2/3: accelerations of the previous evaluation
     const int *run_flag;                  // when set: the walk runs only if *run_flag != 0
     int flush_at;                         // lists are evaluated once they hold more entries (<= 32)
+    const float *rcrit2;                  // MODE 1, treecode1 criteria: accept iff dmin^2 > rcrit2[node]
     const int32_t *sys_root, *body_sys;   // forest: root cell of each group's system
     const MlpSmem *mlp;                   // MODE 3: packed network
     float mlp_threshold;                  // MODE 3: accept iff logit > threshold
@@ -483,7 +484,8 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                         if (logit > g.mlp_threshold) accm = my_mask;
                         else openm = my_mask;
                     } else if (MODE == 1 || (MODE >= 2 && !(amin > 0.f))) {
-                        if (tmin >= dsq) accm = my_mask;
+                        const bool acc = (MODE == 1 && g.rcrit2) ? dmin2 > g.rcrit2[my_node] : tmin >= dsq;
+                        if (acc) accm = my_mask;
                         else openm = my_mask;
                     } else if (MODE == 3) {
                         const float4 Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
@@ -735,6 +737,7 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     if (ntarget <= 0) return HC_OK;
     WalkArgs a;
     a.run_flag = run_flag;
+    a.rcrit2 = nullptr;
     {
         const int depth = c->list_depth >= 32 && c->list_depth <= BCAP ? c->list_depth : BCAP;
         a.flush_at = depth - 32;          // an iteration appends at most 32 entries
@@ -781,7 +784,10 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     const bool count = c->prm.count_per_body && self && c->cnt_b;
     const int v = (c->prm.usequad ? 2 : 0) + (count ? 1 : 0);
     a.eps_acc = (float)c->group_theta;
-    if (!body_rule && c->criterion == HC_CRITERION_GROUP) {
+    const bool rc = c->criterion == HC_CRITERION_BH86 || c->criterion == HC_CRITERION_SW94 ||
+                    c->criterion == HC_CRITERION_BARNES;
+    if (!body_rule && (c->criterion == HC_CRITERION_GROUP || rc)) {
+        if (rc) a.rcrit2 = c->rcrit2;
         a.tol2d = c->group_theta * c->group_theta;
         a.tol2f = (float)a.tol2d;
         switch (v) {

@@ -307,7 +307,7 @@ class Context:
         """'body' (the reference's per-body rule), or one decision per 32-body group: 'group' (opening
         angle theta), 'error' (truncation-error budget theta |a|), 'learned' (the network in the error
         rule's band)."""
-        code = {"body": 0, "group": 1, "error": 2, "learned": 3}[criterion]
+        code = {"body": 0, "group": 1, "error": 2, "learned": 3, "bh86": 4, "sw94": 5, "barnes": 6}[criterion]
         self._check(self._L.hc_set_criterion(self._h, code, float(theta)))
 
     def set_grouping(self, kind: str = "consecutive"):
