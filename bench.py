@@ -57,6 +57,7 @@ def generate(hc, wl, n):
 
 def workload_config(n, mode=("body", TOL), wl="plummer"):
     crit = {"body": "fixed-theta (grav.c subdivp)", "error": "error-bound group rule",
+            "barnes": "treecode1 critical radius in a group walk",
             "learned": "learned opening criterion (guarded)"}[mode[0]]
     w = WORKLOADS[wl]
     what = w["what"].format(n=n, seed=w["seed"])
@@ -227,6 +228,9 @@ def set_mode(ctx, mode):
     if mode[0] == "body":
         ctx.set_params(tol=mode[1])
         ctx.set_criterion("body")
+    elif mode[0] == "barnes":
+        ctx.set_params(tol=TOL)
+        ctx.set_criterion("barnes", mode[1])
     elif mode[0] == "error":
         ctx.set_params(tol=TOL)
         ctx.set_criterion("error", mode[1])
@@ -351,6 +355,7 @@ def run_ours(args, world, rank, local):
     learned_mode = lambda e: ("learned", e, LEARNED_THRESHOLD)
     err_pt, cal_err = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, target)
     lrn_pt, cal_lrn = calibrate(ctx, idx, ea, learned_mode, 1e-3, 64.0, target)
+    tc1_pt, cal_tc1 = calibrate(ctx, idx, ea, lambda t: ("barnes", t), 0.1, 1.5, target, geometric=False)
     th_pt2, cal_th = calibrate(ctx, idx, ea, lambda t: ("body", t), TOL, 1.2, RMS_BUDGET, geometric=False)
     err_pt2, cal_err2 = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, RMS_BUDGET)
     lrn_pt2, cal_lrn2 = calibrate(ctx, idx, ea, learned_mode, 1e-3, 64.0, RMS_BUDGET)
@@ -367,9 +372,11 @@ def run_ours(args, world, rank, local):
         ws = ctx.walk_stats()
         comp = {"fixed_theta_0.5": timed(ctx, ("body", TOL), args.steps, args.warmup, flush, world)}
         comp["fixed_theta_0.5"]["rms"] = sample_error(ctx, idx, ea)[0]
-        if err_pt:
-            comp["error_rule"] = timed(ctx, tuple(err_pt["mode"]), args.steps, args.warmup, flush, world)
-            comp["error_rule"]["rms"] = sample_error(ctx, idx, ea)[0]
+        for name, pt in (("error_rule", err_pt), ("treecode1_new_rcrit", tc1_pt)):
+            if pt:
+                comp[name] = timed(ctx, tuple(pt["mode"]), args.steps, args.warmup, flush, world)
+                comp[name]["rms"] = sample_error(ctx, idx, ea)[0]
+                comp[name]["mode"] = pt["mode"]
         for name, pt in (("fixed_theta_at_1e-3", th_pt2), ("error_rule_at_1e-3", err_pt2),
                          ("learned_at_1e-3", lrn_pt2)):
             if pt:
@@ -385,6 +392,9 @@ def run_ours(args, world, rank, local):
     ratios = {"learned_vs_fixed_theta_equal_rms": value / fixed_value}
     if "error_rule" in comp:
         ratios["error_rule_vs_fixed_theta_equal_rms"] = comp["error_rule"]["bodies_per_s"] / fixed_value
+    if "treecode1_new_rcrit" in comp:
+        ratios["treecode1_group_vs_fixed_theta_equal_rms"] = (comp["treecode1_new_rcrit"]["bodies_per_s"]
+                                                              / fixed_value)
     if "learned_at_1e-3" in comp and "fixed_theta_at_1e-3" in comp:
         ratios["learned_vs_fixed_theta_at_rms_1e-3"] = (comp["learned_at_1e-3"]["bodies_per_s"]
                                                         / comp["fixed_theta_at_1e-3"]["bodies_per_s"])
@@ -447,7 +457,7 @@ def run_ours(args, world, rank, local):
                      "target_rms": target, "guard": guard, "build_ms": head["build_ms"],
                      "walk_ms": head["walk_ms"], "interactions": head["n2b"] + head["nbc"]},
         "comparisons": comp,
-        "calibration": {"fixed_theta_0.5": fixed, "error_rule": cal_err, "learned": cal_lrn,
+        "calibration": {"fixed_theta_0.5": fixed, "error_rule": cal_err, "learned": cal_lrn, "treecode1": cal_tc1,
                         "fixed_theta_1e-3": cal_th, "error_rule_1e-3": cal_err2, "learned_1e-3": cal_lrn2},
         "training": train,
         "tuning": {"fixed_theta": tuned, "group_criteria": TUNING["group"]},
