@@ -355,7 +355,7 @@ def run_ours(args, world, rank, local):
     learned_mode = lambda e: ("learned", e, LEARNED_THRESHOLD)
     err_pt, cal_err = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, target)
     lrn_pt, cal_lrn = calibrate(ctx, idx, ea, learned_mode, 1e-3, 64.0, target)
-    tc1_pt, cal_tc1 = calibrate(ctx, idx, ea, lambda t: ("barnes", t), 0.1, 1.5, target, geometric=False)
+    tc1_pt, cal_tc1 = calibrate(ctx, idx, ea, lambda t: ("barnes", t), 0.3, 1.5, target, geometric=False)
     th_pt2, cal_th = calibrate(ctx, idx, ea, lambda t: ("body", t), TOL, 1.2, RMS_BUDGET, geometric=False)
     err_pt2, cal_err2 = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, RMS_BUDGET)
     lrn_pt2, cal_lrn2 = calibrate(ctx, idx, ea, learned_mode, 1e-3, 64.0, RMS_BUDGET)
