@@ -412,10 +412,14 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                 }
             }
             // ---- gather up to 32 candidates from the top of the stack ----
-            while (!mlp_round && ncand < 32 && sp > 0) {
+            // Near the stack's capacity take one node at a time: an iteration
+            // then adds at most one entry, so the stack stays within capacity
+            // for any tree depth (32 candidates that all open add up to 28).
+            const int gmax = sp > STACK - 40 ? 1 : 32;
+            while (!mlp_round && ncand < gmax && sp > 0) {
                 const uint2 e = S.stack[sp - 1];
                 const int start = (int)(e.x >> 3), ecnt = (int)(e.x & 7u) + 1;
-                const int take = min(ecnt, 32 - ncand);
+                const int take = min(ecnt, gmax - ncand);
                 const int rel = lane - ncand;
                 if (rel >= 0 && rel < take) {
                     my_node = start + ecnt - take + rel;

@@ -80,3 +80,21 @@ def test_cell_body_counts_reach_the_features(hc):
     # feature 7 = log2(bodies in the cell) / 8: band cells hold from 2 to many bodies
     f7 = x[:, 7]
     assert f7.min() >= 0.124 and f7.max() > 0.5 and len(np.unique(f7)) > 5, (f7.min(), f7.max())
+
+
+def test_small_theta_keeps_the_stack_bounded(hc):
+    """At small theta the group walk opens almost every cell; near the stack's
+    capacity it takes one node at a time instead of failing."""
+    n = 262144
+    m, ph = hc.mkplummer(n, 8)
+    ctx = hc.Context(n, tol=0.5, eps=0.01, usequad=True)
+    ctx.upload(m, ph)
+    ctx.evaluate()
+    idx = np.arange(0, n, 64, dtype=np.int64)
+    ea, _ = ctx.direct_sample(idx)
+    ctx.set_criterion("barnes", 0.3)
+    i3, e3 = _err(ctx, idx, ea)
+    ctx.set_criterion("barnes", 0.15)
+    i2, e2 = _err(ctx, idx, ea)
+    assert ctx.walk_stats()["max_stack"] <= 256
+    assert e2 < e3 and i2 > i3, (e2, e3, i2, i3)
