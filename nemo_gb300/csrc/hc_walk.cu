@@ -63,6 +63,7 @@ struct WarpSmem {
     float4 cq0[CCAP];           // Qxx Qxy Qxz Qyy
     float4 cq1[CCAP];           // Qyz Qzz mask(bits) 0
     unsigned long long stat[8]; // warp totals (lane 0 writes): see the ST_* indices
+    float gu[16];               // the group's uniform values (see GU_* below), read where used
 };
 enum { ST_N2B, ST_NBC, ST_CAND, ST_MIXED, ST_EB, ST_EC, ST_MLP, ST_ROUNDS };
 
@@ -245,9 +246,9 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
 //         cell's bodies; p = 3 with quadrupoles, 2 without), is at most
 //         eps_acc times the group's smallest |a| of the previous evaluation.
 template <bool QUAD, bool COUNT, int MODE>
-// Register budget: 96 (5 blocks of 4 warps per SM) for the fixed rules; the
-// learned walk's inline network round needs 128 (4 blocks).
-__global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs g)
+// Register budget: 96 (5 blocks of 4 warps per SM) for the per-body rule and
+// the learned walk, 80 (6 blocks) for the group and error rules.
+__global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_walk(WalkArgs g)
 {
     if (g.run_flag && *g.run_flag == 0) return;   // guard passed: no fallback walk
     extern __shared__ float4 smem_raw[];
@@ -314,6 +315,19 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
             amin = wmin(valid ? __double2float_rn(sqrt(axo * axo + ayo * ayo + azo * azo)) : 3.0e38f);
         }
         const float cR = 2e-6f * tol2 * rg2;     // absolute band term of the FP32 decision
+        // Under the group criteria the traversal loop reads these warp-uniform
+        // values from shared memory (volatile: not kept in registers), which
+        // leaves its registers to the per-lane state; the per-body rule, which
+        // reads them per lane in every mixed test, keeps them in registers.
+        volatile float *gu = S.gu;
+#define GUV(i, reg) (MODE == 0 ? (reg) : gu[i])
+        __syncwarp();
+        if (lane == 0) {
+            const float v[15] = {ghx, ghy, ghz, glx, gly, glz, gminx, gmaxx, gminy, gmaxy, gminz, gmaxz, rg2, amin, cR};
+#pragma unroll
+            for (int k = 0; k < 15; k++) gu[k] = v[k];
+        }
+        __syncwarp();
 
         float sphi = 0.f, sax = 0.f, say = 0.f, saz = 0.f;   // Kahan sums
         float cphi = 0.f, cax = 0.f, cay = 0.f, caz = 0.f;
@@ -449,9 +463,9 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                 if (have) {
                     const float4 Q0 = g.nodeQ[2 * (int64_t)my_node], Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
                     float f[12];
-                    cell_features_inl(f, q_dmin2, q_dmax2, B.w, A.w, Q1.w, sqrtf(q_dmin2) - Q1.w, Q0, Q1, amin, rg2,
+                    cell_features_inl(f, q_dmin2, q_dmax2, B.w, A.w, Q1.w, sqrtf(q_dmin2) - Q1.w, Q0, Q1, GUV(13, amin), GUV(12, rg2),
                                       eps2, C.y >> 8, (int)cnt,
-                                      __log2f(fmaxf(q_err, 1e-38f)) - __log2f(g.eps_acc * amin));
+                                      __log2f(fmaxf(q_err, 1e-38f)) - __log2f(g.eps_acc * GUV(13, amin)));
 #pragma unroll
                     for (int k = 0; k < 6; k++) w[k] = pack_bf16(f[2 * k], f[2 * k + 1]);
                 }
@@ -462,7 +476,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                 __syncwarp();
                 logit = mlp_warp_lean(*g.mlp, Qs->x, Qs->z, ncand);
             }
-            const float cx = (A.x - ghx) + (B.x - glx), cy = (A.y - ghy) + (B.y - gly), cz = (A.z - ghz) + (B.z - glz);
+            const float cx = (A.x - GUV(0, ghx)) + (B.x - GUV(3, glx)), cy = (A.y - GUV(1, ghy)) + (B.y - GUV(4, gly)), cz = (A.z - GUV(2, ghz)) + (B.z - GUV(5, glz));
             const bool isbody = C.x < 0;
             unsigned openm = 0, accm = 0;
             bool mixed = false;
@@ -475,19 +489,19 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                     accm = my_mask & ~self;
                 } else {
                     const float dsq = B.w;
-                    const float ex = fmaxf(0.f, fmaxf(gminx - cx, cx - gmaxx));
-                    const float ey = fmaxf(0.f, fmaxf(gminy - cy, cy - gmaxy));
-                    const float ez = fmaxf(0.f, fmaxf(gminz - cz, cz - gmaxz));
-                    const float fx = fmaxf(fabsf(cx - gminx), fabsf(cx - gmaxx));
-                    const float fy = fmaxf(fabsf(cy - gminy), fabsf(cy - gmaxy));
-                    const float fz = fmaxf(fabsf(cz - gminz), fabsf(cz - gmaxz));
+                    const float ex = fmaxf(0.f, fmaxf(GUV(6, gminx) - cx, cx - GUV(7, gmaxx)));
+                    const float ey = fmaxf(0.f, fmaxf(GUV(8, gminy) - cy, cy - GUV(9, gmaxy)));
+                    const float ez = fmaxf(0.f, fmaxf(GUV(10, gminz) - cz, cz - GUV(11, gmaxz)));
+                    const float fx = fmaxf(fabsf(cx - GUV(6, gminx)), fabsf(cx - GUV(7, gmaxx)));
+                    const float fy = fmaxf(fabsf(cy - GUV(8, gminy)), fabsf(cy - GUV(9, gmaxy)));
+                    const float fz = fmaxf(fabsf(cz - GUV(10, gminz)), fabsf(cz - GUV(11, gmaxz)));
                     const float dmin2 = ex * ex + ey * ey + ez * ez;
                     const float dmax2 = fx * fx + fy * fy + fz * fz;
                     const float tmin = tol2 * dmin2, tmax = tol2 * dmax2;
                     if (MODE == 3 && mlp_round) {
                         if (logit > g.mlp_threshold) accm = my_mask;
                         else openm = my_mask;
-                    } else if (MODE == 1 || (MODE >= 2 && !(amin > 0.f))) {
+                    } else if (MODE == 1 || (MODE >= 2 && !(GUV(13, amin) > 0.f))) {
                         const bool acc = (MODE == 1 && g.rcrit2) ? dmin2 > g.rcrit2[my_node] : tmin >= dsq;
                         if (acc) accm = my_mask;
                         else openm = my_mask;
@@ -500,7 +514,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                             const float gi = 1.f / gap, bg = b * gi;
                             err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
                         }
-                        const float budget = g.eps_acc * amin;
+                        const float budget = g.eps_acc * GUV(13, amin);
                         if (err < budget * g.band_lo_f) accm = my_mask;          // below the band
                         else if (err > budget * g.band_hi_f) openm = my_mask;    // above it
                         else if (g.collect) {
@@ -513,11 +527,11 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                                 if (slot < g.sample_cap) {
                                     float f[12];
                                     cell_features(f, dmin2, dmax2, dsq, A.w, b, gap, g.nodeQ[2 * (int64_t)my_node], Q1,
-                                                  amin, rg2, eps2, C.y >> 8, (int)cnt, p_raw);
+                                                  GUV(13, amin), GUV(12, rg2), eps2, C.y >> 8, (int)cnt, p_raw);
                                     for (int k = 0; k < 12; k++) g.sample_x[(int64_t)slot * 12 + k] = f[k];
                                     g.sample_group[slot] = (int)grp;
                                     g.sample_node[slot] = my_node;
-                                    g.sample_amin[slot] = amin;
+                                    g.sample_amin[slot] = GUV(13, amin);
                                 }
                             }
                         } else {
@@ -534,12 +548,12 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                         if (acc_ok) {
                             const float gi = 1.f / gap, bg = b * gi;
                             const float err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
-                            acc_ok = err <= g.eps_acc * amin;
+                            acc_ok = err <= g.eps_acc * GUV(13, amin);
                         }
                         if (acc_ok) accm = my_mask;
                         else openm = my_mask;
-                    } else if (tmin - dsq > 8e-6f * tmin + cR) accm = my_mask;  // every body accepts
-                    else if (dsq - tmax > 8e-6f * tmax + cR) openm = my_mask;    // every body opens
+                    } else if (tmin - dsq > 8e-6f * tmin + GUV(14, cR)) accm = my_mask;  // every body accepts
+                    else if (dsq - tmax > 8e-6f * tmax + GUV(14, cR)) openm = my_mask;    // every body opens
                     else mixed = true;
                 }
             }
@@ -574,7 +588,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                 const float d2 = dx * dx + dy * dy + dz * dz;
                 const float t = tol2 * d2 - jd;
                 bool op = t < 0.f;
-                if (in && fabsf(t) <= 8e-6f * tol2 * d2 + cR) {
+                if (in && fabsf(t) <= 8e-6f * tol2 * d2 + GUV(14, cR)) {
                     // borderline: decide exactly as subdivp does, in FP64
                     op = open_exact(g.ncx[jn], g.ncy[jn], g.ncz[jn], xd, yd, zd, g.tol2d, g.box->dsq[jdepth]);
                     nborder++;
@@ -608,11 +622,11 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
                 // node - centre as an unevaluated float sum hi + lo (TwoSum of the hi parts)
                 const int pos = nb + __popc(bbal & lt);
                 float hx, hy, hz, ex, ey, ez;
-                two_diff(A.x, ghx, hx, ex);
-                two_diff(A.y, ghy, hy, ey);
-                two_diff(A.z, ghz, hz, ez);
+                two_diff(A.x, GUV(0, ghx), hx, ex);
+                two_diff(A.y, GUV(1, ghy), hy, ey);
+                two_diff(A.z, GUV(2, ghz), hz, ez);
                 S.bl[pos] = make_float4(hx, hy, hz, A.w);
-                S.bl2[pos] = make_float4(ex + (B.x - glx), ey + (B.y - gly), ez + (B.z - glz), __uint_as_float(accm));
+                S.bl2[pos] = make_float4(ex + (B.x - GUV(3, glx)), ey + (B.y - GUV(4, gly)), ez + (B.z - GUV(5, glz)), __uint_as_float(accm));
                 gb += __popc(accm);
             }
             if (ac) {
@@ -640,6 +654,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 3 ? 4 : 5) k_walk(WalkArgs
             }
             __syncwarp();
         }
+#undef GUV
         if (overflow) {
             if (lane == 0) {
                 atomicCAS(&g.st->error, 0, HC_ERR_STACK);
