@@ -553,6 +553,87 @@ def run_ensemble(args, world, rank, local):
         print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------- composite galaxy workload
+
+GAL_N = (4194304, 1048576, 11534336)      # disk, bulge, halo: 2^24 bodies
+GAL_SEED, GAL_EPS, GAL_DT = 11, 0.01, 1.0 / 512
+
+
+def angular_momentum(d):
+    a = np.array(d.amten).reshape(3, 3)      # antisymmetric: L = (A_yz, A_zx, A_xy)
+    return np.array([a[1, 2], a[2, 0], a[0, 1]])
+
+
+def run_galaxy(args, world, rank, local):
+    """Leapfrog steps of the composite disk galaxy with the learned criterion
+    (calibrated to the fixed-theta rule's RMS error, guard on), each step one
+    CUDA-graph replay (build, walk with the closing half-kick, diagnostics),
+    then kick-drift; FP64 energy and angular-momentum drift."""
+    import torch
+    from nemo_gb300 import build as B
+    B.build()
+    from nemo_gb300 import hackcode as hc
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (the CUDA path has no CPU fallback)")
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    m, ph = hc.mkgalaxy(*GAL_N, seed=GAL_SEED)
+    t_gen = time.perf_counter() - t0
+    n = len(m)
+    ctx = hc.Context(n, tol=TOL, eps=GAL_EPS, fcells=1.0, usequad=USEQUAD)
+    ctx.upload(m, ph)
+    ctx.evaluate()
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(n, size=min(args.sample, 4096), replace=False)).astype(np.int64)
+    ea, _ = ctx.direct_sample(idx)
+    train = ctx.learn_from_self(theta=0.03, target=1 << 20)
+    ctx.learn_band(0.5, 3.0)
+    fixed = point(ctx, ("body", TOL), idx, ea)
+    lrn_pt, cal = calibrate(ctx, idx, ea, lambda e: ("learned", e, LEARNED_THRESHOLD), 1e-3, 64.0, fixed["rms"],
+                            steps=5)
+    mode = tuple(lrn_pt["mode"]) if lrn_pt else ("body", TOL)
+    set_mode(ctx, mode)
+    ctx.set_guard(GUARD_SAMPLE, RMS_BUDGET, seed=1)
+    # start the run from the initial conditions
+    ctx.upload(m, ph)
+    d0, _, _, _ = ctx.step(GAL_DT, 0)
+    e0, l0 = d0.etot[0], angular_momentum(d0)
+    for k in range(1, args.warmup + 1):
+        ctx.step(GAL_DT, k)
+    barrier(world)
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for k in range(args.warmup + 1, args.warmup + 1 + args.steps):
+            t1 = time.perf_counter()
+            d, _, _, _ = ctx.step(GAL_DT, k)
+            step_ms.append(1e3 * (time.perf_counter() - t1))
+    barrier(world)
+    guard = ctx.guard_stats()
+    l1 = angular_momentum(d)
+    mean_ms = reduce_max(statistics.mean(step_ms), world)
+    out = {
+        "metric": "composite galaxy leapfrog body-steps/s", "value": world * n / (mean_ms * 1e-3),
+        "unit": "body-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: composite disk galaxy (project generator, ran3 seed=11)",
+        "config": {"workload": f"disk {GAL_N[0]} + Hernquist bulge {GAL_N[1]} + NFW halo {GAL_N[2]} bodies, "
+                               f"eps={GAL_EPS}, dt=1/512, quadrupole, learned criterion (guarded), one CUDA graph "
+                               f"per step", "criterion_setting": list(mode),
+                   "timing": "host wall clock per step (graph replay, synchronised)"},
+        "energy_drift": abs((d.etot[0] - e0) / e0),
+        "angular_momentum_drift": float(np.linalg.norm(l1 - l0) / np.linalg.norm(l0)),
+        "steps_total": args.warmup + 1 + args.steps,
+        "rms_error": {"learned": lrn_pt["rms"] if lrn_pt else None, "fixed_theta_0.5": fixed["rms"],
+                      "sample": int(len(idx))},
+        "evaluation_ms": {"learned": lrn_pt["step_ms"] if lrn_pt else None, "fixed_theta_0.5": fixed["step_ms"]},
+        "calibration": cal, "training": train, "guard": guard, "generator_seconds": t_gen,
+        "clocks": clk.summary(),
+    }
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, world, rank):
@@ -594,9 +675,9 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stats", action="store_true", help="one extra counting walk: mask popcount histogram")
-    ap.add_argument("--workload", default="plummer", choices=["plummer", "hernquist", "ensemble"],
+    ap.add_argument("--workload", default="plummer", choices=["plummer", "hernquist", "ensemble", "galaxy"],
                     help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
-                         "ensemble: 4096 independent systems")
+                         "ensemble: 4096 independent systems; galaxy: 2^24-body disk galaxy, leapfrog")
     ap.add_argument("--nsys", type=int, default=ENS_NSYS)
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -604,6 +685,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "ensemble":
         run_ensemble(args, world, rank, local)
+    elif args.workload == "galaxy":
+        run_galaxy(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

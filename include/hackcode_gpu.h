@@ -289,6 +289,13 @@ void hc_make_testdata(int n, int seed, int cencon, double *mass, double *phase);
  * distribution function (Hernquist 1990, eq. 17), equal masses M(rtrunc)/n,
  * centre of mass at rest at the origin; ran3 seeded with seed. */
 void hc_mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase);
+/* Composite disk galaxy, G = 1 (no counterpart in hackcode1; NEMO's mkexpdisk,
+ * mkhalo and magalie differ): exponential sech^2 disk (M 0.1, R_d 1, z0 0.1,
+ * Toomre Q 1.5 epicyclic velocities), Hernquist bulge (M 0.033, a 0.2) and
+ * NFW halo (M_vir 1, c 10, r_vir 30, truncated at r_vir) with isotropic
+ * velocities from Eddington's inversion in the total potential; bodies in
+ * the order disk, bulge, halo; ran3 seeded with seed. */
+void hc_mkgalaxy(int64_t n_disk, int64_t n_bulge, int64_t n_halo, int seed, double *mass, double *phase);
 
 /* Host services of the drop-in programs, exported for tests: copy every
  * snapshot of a filestruct file through the reader and writer (returns the

@@ -26,7 +26,7 @@ ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "cell pool exhausted", -4: "
 EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_upload", "hc_set_box", "hc_get_box",
            "hc_build_tree", "hc_tree_summary", "hc_dump_tree", "hc_forces", "hc_forces_at", "hc_download",
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
-           "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_mkhernquist", "hc_make_testdata",
+           "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_mkhernquist", "hc_mkgalaxy", "hc_make_testdata",
            "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate",
            "hc_set_graphs", "hc_diagnostics_noalloc", "hc_set_criterion", "hc_set_grouping",
            "hc_learn_nparams", "hc_learn_init", "hc_learn_set_params", "hc_learn_get_params", "hc_learn_infer",
@@ -170,6 +170,8 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_mkplummer.restype = None
     L.hc_mkhernquist.argtypes = [C.c_int, C.c_int, C.c_double, _dp, _dp]
     L.hc_mkhernquist.restype = None
+    L.hc_mkgalaxy.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_int, _dp, _dp]
+    L.hc_mkgalaxy.restype = None
     L.hc_make_testdata.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
     L.hc_make_testdata.restype = None
     L.hc_snapcopy.argtypes = [C.c_char_p, C.c_char_p]
@@ -553,6 +555,16 @@ def mkhernquist(n: int, seed: int = 7, rtrunc: float = 100.0):
     m = np.zeros(n)
     ph = np.zeros((n, 2, 3))
     library().hc_mkhernquist(int(n), int(seed), float(rtrunc), m, ph)
+    return m, ph
+
+
+def mkgalaxy(n_disk: int = 4194304, n_bulge: int = 1048576, n_halo: int = 11534336, seed: int = 11):
+    """Composite disk galaxy (exponential disk, Hernquist bulge, NFW halo): (mass[n], phase[n,2,3]),
+    bodies in the order disk, bulge, halo."""
+    n = int(n_disk) + int(n_bulge) + int(n_halo)
+    m = np.zeros(n)
+    ph = np.zeros((n, 2, 3))
+    library().hc_mkgalaxy(int(n_disk), int(n_bulge), int(n_halo), int(seed), m, ph)
     return m, ph
 
 

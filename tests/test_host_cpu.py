@@ -187,3 +187,42 @@ def test_mkhernquist_moments():
     vr2 = np.mean((np.sum(x * v, 1) / rr) ** 2)
     vt2 = np.mean((v ** 2).sum(1)) - vr2
     assert abs(vt2 / (2 * vr2) - 1.0) < 0.02, vt2 / (2 * vr2)   # isotropic
+
+
+def test_mkgalaxy_moments():
+    """The composite galaxy generator (no reference counterpart, parity
+    unpinned): component masses, the disk's exponential scale length and
+    sech^2 thickness, rotation, the halo's NFW mass profile and the bulge and
+    halo velocity dispersions against the isotropic Jeans equation in the
+    same spherical potential."""
+    from nemo_gb300 import hackcode as hc
+    nd, nb, nh = 100000, 40000, 200000
+    m, ph = hc.mkgalaxy(nd, nb, nh, 11)
+    x, v = ph[:, 0], ph[:, 1]
+    d, b, h = slice(0, nd), slice(nd, nd + nb), slice(nd + nb, None)
+    np.testing.assert_allclose([m[d].sum(), m[b].sum(), m[h].sum()], [0.1, 0.033, 1.0], rtol=1e-12)
+    # centre: the disk's mid-plane (the total centre of mass is at the origin)
+    c = np.median(x[d], axis=0)
+    R = np.hypot(x[d, 0] - c[0], x[d, 1] - c[1])
+    assert abs(R.mean() - 2.0) < 0.02                                   # <R> = 2 R_d
+    assert abs(np.mean(np.abs(x[d, 2] - c[2])) - 0.1 * np.log(2)) < 0.002   # sech^2: <|z|> = z0 ln 2
+    lz = (x[d, 0] - c[0]) * v[d, 1] - (x[d, 1] - c[1]) * v[d, 0]
+    assert np.mean(lz > 0) > 0.95                                       # rotating about +z
+    rh = np.linalg.norm(x[h] - c, axis=1)
+    nfw = lambda y: np.log1p(y) - y / (1 + y)
+    assert abs(np.mean(rh < 3.0) - nfw(1.0) / nfw(10.0)) < 0.005
+    assert rh.max() < 30.5
+    # isotropic Jeans: rho sigma^2(r) = int_r^rvir rho G M_tot / r'^2 dr'
+    rr = np.logspace(-4, np.log10(30.0), 4000)
+    mb = 0.033 * (rr / (rr + 0.2)) ** 2 / (30.0 / 30.2) ** 2
+    mh = nfw(rr / 3.0) / nfw(10.0)
+    md = 0.1 * (1 - (1 + rr) * np.exp(-rr)) / (1 - 16 * np.exp(-15))
+    mt = mb + mh + md
+    for sl, rho, r0 in ((b, lambda r: 0.2 / (r * (r + 0.2) ** 3), 0.3), (h, lambda r: 1 / (r / 3 * (1 + r / 3) ** 2), 3.0)):
+        w = rho(rr) * mt / rr ** 2
+        k = np.searchsorted(rr, r0)
+        s2 = np.trapezoid(w[k:], rr[k:]) / rho(rr[k])
+        r = np.linalg.norm(x[sl] - c, axis=1)
+        sel = (r > 0.9 * r0) & (r < 1.1 * r0)
+        meas = np.mean(np.sum(v[sl][sel] ** 2, axis=1)) / 3
+        assert abs(meas / s2 - 1) < 0.08, (r0, meas, s2)
