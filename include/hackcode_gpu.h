@@ -327,7 +327,8 @@ int hc_diagnostics_noalloc(int64_t n, const double *mass, const double *x, const
  * (each in its own slot of a forest box, with its own persistent expandbox
  * root box starting at (-2,-2,-2), 4) and are walked with the per-body rule
  * at tol; the others use an FP32 direct sum, one thread block per system.
- * Arrays are the systems' bodies concatenated in the given order. */
+ * Arrays are the systems' bodies concatenated in the given order; every
+ * body needs a positive mass (hc_ens_upload returns HC_ERR_ARG otherwise). */
 #define HC_ENS_DIRECT_LIMIT 4096
 typedef struct hc_ens hc_ens;
 typedef struct {

@@ -588,8 +588,10 @@ int hc_ens_upload(hc_ens *e, const double *mass, const double *phase)
         std::memcpy(&ph[6 * e->int_off[k]], phase + 6 * e->user_off[u], sizeof(double) * 6 * cnt);
     }
     for (int64_t i = 0; i < n; i++)
-        if (!std::isfinite(m[i])) {
-            e->err = "non-finite mass";
+        if (!std::isfinite(m[i]) || !(m[i] > 0.0)) {
+            // a massless body is walked in a run of 32 with its neighbours in
+            // key order, which may belong to another system
+            e->err = "ensemble bodies need positive, finite masses";
             return HC_ERR_ARG;
         }
     if (!e->d_stage) HC_TRY(ens_alloc(e->err, &e->d_stage, 6 * n));

@@ -1,0 +1,138 @@
+"""GPU edge cases of the additions: ensembles that are all-direct, all-tree or
+a single system, the rejection of massless ensemble bodies, caller-order
+independence of ensemble results, and the approximate criteria and the guard
+without quadrupoles."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def hc():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from nemo_gb300 import build as B
+    B.build()
+    from nemo_gb300 import hackcode
+    return hackcode
+
+
+def _systems(hc, counts, seed0=200):
+    ms, phs = [], []
+    for i, n in enumerate(counts):
+        m, ph = hc.mkplummer(int(n), seed0 + i)
+        ms.append(m)
+        phs.append(ph)
+    return ms, phs
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
+
+
+@pytest.mark.parametrize("direct_max", [0, 4096])
+def test_ensemble_all_tree_or_all_direct(hc, direct_max):
+    counts = [1500, 2100, 3000]
+    ms, phs = _systems(hc, counts)
+    ens = hc.Ensemble(counts, tol=0.6, eps=0.02, usequad=True, direct_max=direct_max)
+    ens.upload(np.concatenate(ms), np.concatenate(phs))
+    ens.step(1 / 256, 0)
+    _, acc, _ = ens.download(phase=False, phi=False)
+    info = ens.info()
+    assert (info["nsys_tree"], info["nsys_direct"]) == ((3, 0) if direct_max == 0 else (0, 3))
+    off = np.concatenate([[0], np.cumsum(counts)])
+    for s, n in enumerate(counts):
+        ctx = hc.Context(n, tol=0.6, eps=0.02, usequad=True)
+        ctx.upload(ms[s], phs[s])
+        ctx.evaluate()
+        ref, _ = ctx.direct_sample(np.arange(n, dtype=np.int64))
+        if direct_max == 0:
+            ctx.set_grouping("tree")
+            ctx.evaluate()
+            _, ref, _ = ctx.download(phase=False, phi=False)
+            assert np.quantile(_rel(acc[off[s]:off[s + 1]], ref), 0.999) < 1e-5
+        else:
+            assert _rel(acc[off[s]:off[s + 1]], ref).max() < 1e-5
+        ctx.close()
+    ens.close()
+
+
+def test_ensemble_single_system_and_order(hc):
+    counts = [5000, 700, 2500]
+    ms, phs = _systems(hc, counts, 300)
+    e1 = hc.Ensemble(counts, tol=0.6, eps=0.02, direct_max=1024)
+    e1.upload(np.concatenate(ms), np.concatenate(phs))
+    e1.step(1 / 256, 0)
+    _, a1, p1 = e1.download(phase=False)
+    # the same systems in another order give the same per-system results
+    perm = [2, 0, 1]
+    c2 = [counts[i] for i in perm]
+    e2 = hc.Ensemble(c2, tol=0.6, eps=0.02, direct_max=1024)
+    e2.upload(np.concatenate([ms[i] for i in perm]), np.concatenate([phs[i] for i in perm]))
+    e2.step(1 / 256, 0)
+    _, a2, p2 = e2.download(phase=False)
+    o1 = np.concatenate([[0], np.cumsum(counts)])
+    o2 = np.concatenate([[0], np.cumsum(c2)])
+    for j, i in enumerate(perm):
+        np.testing.assert_allclose(a2[o2[j]:o2[j + 1]], a1[o1[i]:o1[i + 1]], rtol=1e-5, atol=1e-9)
+        np.testing.assert_allclose(p2[o2[j]:o2[j + 1]], p1[o1[i]:o1[i + 1]], rtol=1e-5)
+    # one system alone
+    e3 = hc.Ensemble([counts[0]], tol=0.6, eps=0.02, direct_max=1024)
+    e3.upload(ms[0], phs[0])
+    e3.step(1 / 256, 0)
+    _, a3, _ = e3.download(phase=False, phi=False)
+    assert np.quantile(_rel(a3, a1[:counts[0]]), 0.999) < 1e-5
+    for e in (e1, e2, e3):
+        e.close()
+
+
+def test_ensemble_rejects_massless_bodies(hc):
+    counts = [3000, 2000]
+    ms, phs = _systems(hc, counts, 400)
+    ms[0][::10] = 0.0
+    ens = hc.Ensemble(counts, tol=0.6, eps=0.02, direct_max=1024)
+    with pytest.raises(hc.HCError):
+        ens.upload(np.concatenate(ms), np.concatenate(phs))
+    ens.close()
+
+
+@pytest.mark.parametrize("criterion,value", [("error", 0.03), ("barnes", 0.6), ("bh86", 0.6), ("sw94", 0.6)])
+def test_criteria_without_quadrupoles(hc, criterion, value):
+    n = 65536
+    m, ph = hc.mkplummer(n, 9)
+    ctx = hc.Context(n, tol=0.5, eps=0.01, usequad=False)
+    ctx.upload(m, ph)
+    ctx.evaluate()
+    idx = np.arange(0, n, 32, dtype=np.int64)
+    ea, _ = ctx.direct_sample(idx)
+    ctx.set_criterion(criterion, value)
+    ctx.set_guard(256, 1e-2, seed=2)
+    ctx.evaluate()
+    ctx.evaluate()
+    _, acc, _ = ctx.download(phase=False, phi=False)
+    rel = _rel(acc[idx], ea)
+    st = ctx.guard_stats()
+    assert np.sqrt(np.mean(rel ** 2)) < 1e-2 and st["trips"] == 0, (np.sqrt(np.mean(rel ** 2)), st)
+    assert st["last_rms"] < 1e-2
+
+
+def test_learned_without_quadrupoles(hc):
+    n = 131072
+    m, ph = hc.mkplummer(n, 10)
+    ctx = hc.Context(n, tol=0.5, eps=0.01, usequad=False)
+    ctx.upload(m, ph)
+    ctx.evaluate()
+    idx = np.arange(0, n, 64, dtype=np.int64)
+    ea, _ = ctx.direct_sample(idx)
+    info = ctx.learn_from_self(theta=0.03, target=1 << 17)
+    assert info["samples"] > 5000 and info["train_accuracy"] > 0.7
+    ctx.learn_band(0.5, 3.0)
+    ctx.set_criterion("learned", 0.03)
+    ctx.evaluate()
+    ctx.evaluate()
+    _, acc, _ = ctx.download(phase=False, phi=False)
+    rms = np.sqrt(np.mean(_rel(acc[idx], ea) ** 2))
+    assert rms < 3e-3, rms
+    assert ctx.walk_stats()["network"] > 0
