@@ -506,32 +506,32 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             cx = ddiv(cx, m);
             cy = ddiv(cy, m);
             cz = ddiv(cz, m);
-            // bmax: radius around the centre of mass holding every body of the
-            // cell (children's extents shifted to the new centre)
+            float4 A, B;
+            split_hilo(cx, &A.x, &B.x);
+            split_hilo(cy, &A.y, &B.y);
+            split_hilo(cz, &A.z, &B.z);
+            // children's offsets from the centre of mass in FP32, from the
+            // hi + lo positions ((hi - hi) + (lo - lo)): no FP64 work per child.
+            // bmax: children's extents shifted to the new centre; Q = sum_child
+            // [ m (3 dr dr^T - |dr|^2 I) + Q_child ], dr = x_child - x_cm
             float bmax = 0.f, nbody = 0.f;
+            float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             for (int i = 0; i < nc; i++) {
                 const int ch = fc + i;
-                const float dx = __double2float_rn(dsub(ncx[ch], cx)), dy = __double2float_rn(dsub(ncy[ch], cy)),
-                            dz = __double2float_rn(dsub(ncz[ch], cz));
+                const float4 ca = nodeA[ch], cb = nodeB[ch];
+                const float dx = (ca.x - A.x) + (cb.x - B.x), dy = (ca.y - A.y) + (cb.y - B.y),
+                            dz = (ca.z - A.z) + (cb.z - B.z);
                 const bool cell = nodeC[ch].x >= 0;
-                const float4 q1 = cell ? nodeQ[2 * (int64_t)ch + 1] : make_float4(0.f, 0.f, 1.f, 0.f);
-                bmax = fmaxf(bmax, sqrtf(dx * dx + dy * dy + dz * dz) + q1.w);
+                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = make_float4(0.f, 0.f, 1.f, 0.f);
+                if (cell) {
+                    q0 = nodeQ[2 * (int64_t)ch];
+                    q1 = nodeQ[2 * (int64_t)ch + 1];
+                }
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                bmax = fmaxf(bmax, sqrtf(r2) + q1.w);
                 nbody += q1.z;                   // bodies in the cell (exact below 2^24)
-            }
-            // Q = sum_child [ m (3 dr dr^T - |dr|^2 I) + Q_child ], dr = x_child - x_cm
-            float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (usequad) {
-                for (int i = 0; i < nc; i++) {
-                    const int ch = fc + i;
-                    const float mr = __double2float_rn(nm[ch]);
-                    const float dx = __double2float_rn(dsub(ncx[ch], cx)), dy = __double2float_rn(dsub(ncy[ch], cy)),
-                                dz = __double2float_rn(dsub(ncz[ch], cz));
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
-                    if (nodeC[ch].x >= 0) {
-                        q0 = nodeQ[2 * (int64_t)ch];
-                        q1 = nodeQ[2 * (int64_t)ch + 1];
-                    }
+                if (usequad) {
+                    const float mr = ca.w;
                     Q[0] += mr * (3.f * dx * dx - r2) + q0.x;
                     Q[1] += mr * (3.f * dx * dy) + q0.y;
                     Q[2] += mr * (3.f * dx * dz) + q0.z;
@@ -544,10 +544,6 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             ncx[k] = cx;
             ncy[k] = cy;
             ncz[k] = cz;
-            float4 A, B;
-            split_hilo(cx, &A.x, &B.x);
-            split_hilo(cy, &A.y, &B.y);
-            split_hilo(cz, &A.z, &B.z);
             A.w = __double2float_rn(m);
             B.w = dsqf;
             nodeA[k] = A;
