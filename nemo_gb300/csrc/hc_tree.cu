@@ -37,10 +37,20 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// (x - rmin) / rsize.  A power-of-two rsize (hackcode1's box is 4 * 2^k)
+// divides exactly as a multiplication by its reciprocal: the same correctly
+// rounded result, without an FP64 division.
+__device__ __forceinline__ double scaled(double x, double rmin, double rsize)
+{
+    int e;
+    const double f = frexp(rsize, &e);
+    return f == 0.5 ? dmul(dsub(x, rmin), ldexp(1.0, 1 - e)) : ddiv(dsub(x, rmin), rsize);
+}
+
 // intcoord (load.c:135-156): xsc = (x - rmin)/rsize; inside iff 0 <= xsc < 1.
 __device__ __forceinline__ bool intcoord1(double x, double rmin, double rsize, int *xi)
 {
-    double xsc = ddiv(dsub(x, rmin), rsize);
+    double xsc = scaled(x, rmin, rsize);
     if (0.0 <= xsc && xsc < 1.0) {
         *xi = (int)floor(dmul((double)HC_IMAX, xsc));
         return true;
@@ -200,7 +210,7 @@ __device__ __forceinline__ int intcoord_clamped(double x, double rmin, double rs
 {
     int xi;
     if (intcoord1(x, rmin, rsize, &xi)) return xi;
-    double xsc = ddiv(dsub(x, rmin), rsize);
+    double xsc = scaled(x, rmin, rsize);
     return xsc < 0.0 ? 0 : HC_IMAX - 1;   // massless bodies / test points outside the box
 }
 
