@@ -239,6 +239,17 @@ int hc_learn_set_band(hc_ctx *ctx, double lo, double hi);
 enum { HC_GROUPS_CONSECUTIVE = 0, HC_GROUPS_TREE = 1 };
 int hc_set_grouping(hc_ctx *ctx, int kind);
 
+/* External potential added to every body's acceleration and potential after
+ * the walk, as hackcode3 does with potname= / potpars= (hackcode3/grav.c:34-38,
+ * code.c:136-139): NEMO's plug-ins plummer (par: omega, M, a), hernquist
+ * (omega, M, a), miyamoto (omega, M, a, b) and log (omega, m_c, r_c, q, r),
+ * restated on the device with the plug-ins' defaults for missing parameters;
+ * the pattern speed omega must be 0.  The energy in hc_diag counts the
+ * external potential as hackcode3's diagnostics do (code_io.c:180-186).
+ * name NULL, "" or "null" turns it off. */
+enum { HC_EXTPOT_PLUMMER = 1, HC_EXTPOT_HERNQUIST = 2, HC_EXTPOT_MIYAMOTO = 3, HC_EXTPOT_LOG = 4 };
+int hc_set_extpot(hc_ctx *ctx, const char *name, const double *par, int npar);
+
 /* Walk tuning (no counterpart in hackcode1): the largest walk group of tree
  * grouping (1..32 bodies per warp), the interaction-list depth evaluated per
  * flush (32..64 entries) and the grouping kind.  hc_autotune times one

@@ -4,7 +4,8 @@
 // Same keywords, defaults, log table, snapshot stream and state file as
 // src/nbody/evolve/hackcode/hackcode1/code.c:21-191 and code_io.c:35-284.
 // Documented extensions: usequad= (the hackcode1_qp build), dtime= (sets
-// freq = 1/dtime) and nstep= (sets tstop = tnow + nstep/freq).  Interaction
+// freq = 1/dtime), nstep= (sets tstop = tnow + nstep/freq) and hackcode3's
+// potname= / potpars= (an external potential, hackcode3/code.c:136-139).  Interaction
 // counts are 64-bit (the reference's int counters wrap near N=1M).
 #include <cmath>
 #include <cstdio>
@@ -39,6 +40,8 @@ static const char *defv[] = {
     "usequad=false\n        quadrupole moments (the hackcode1_qp build)",
     "dtime=\n               time step; sets freq=1/dtime",
     "nstep=\n               number of steps; sets tstop=tnow+nstep/freq",
+    "potname=\n             external potential, as hackcode3 (plummer, hernquist, miyamoto, log)",
+    "potpars=\n             its parameters, pattern speed first (must be 0)",
     "VERSION=1.5b-gb300\n   GB300 build",
     nullptr,
 };
@@ -276,6 +279,25 @@ int main(int argc, char **argv)
     check(r, hc_upload(r.ctx, r.mass.data(), r.phase.data()), "hc_upload");
     check(r, hc_set_box(r.ctx, r.rmin, r.rsize), "hc_set_box");
     check(r, hc_set_forces(r.ctx, r.acc.data(), r.phi.data()), "hc_set_forces");
+    if (p.has_value("potname")) {                       // hackcode3 code.c:136-139
+        std::vector<double> pars;
+        std::string s = p.get("potpars"), item;
+        for (size_t i = 0; i <= s.size(); i++) {
+            if (i == s.size() || s[i] == ',') {
+                if (!item.empty()) {
+                    int ok = 0;
+                    const double v = hc_nemo_eval(item.c_str(), &ok);
+                    if (!ok) fatal(r.prog, "potpars: cannot parse '" + item + "'");
+                    pars.push_back(v);
+                }
+                item.clear();
+            } else {
+                item += s[i];
+            }
+        }
+        check(r, hc_set_extpot(r.ctx, p.get("potname").c_str(), pars.empty() ? nullptr : pars.data(), (int)pars.size()),
+              "hc_set_extpot");
+    }
 
     // initoutput (code_io.c:64-82)
     fprintf(r.log, "\n%s\n\n", r.headline.c_str());

@@ -75,7 +75,7 @@ void free_all(hc_ctx *c)
     void *mptrs[] = {c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_grad, c->mlp_loss, c->mlp_gpart, c->mlp_lpart,
                      c->mlp_packed, c->sample_count, c->sample_x, c->sample_amin, c->sample_y, c->sample_rel,
                      c->sample_w, c->sample_group, c->sample_node, c->guard_idx, c->guard_part, c->guard,
-                     c->rcrit2};
+                     c->rcrit2, c->phi_ext};
     for (void *p : mptrs)
         if (p) cudaFree(p);
     if (c->h_st) cudaFreeHost(c->h_st);
@@ -569,6 +569,7 @@ static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bo
         HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
                               nstep, &c->guard->flag, true));
     }
+    if (c->extpot) hc_extpot_launch(c, kick_dthf, nstep);
     HC_CUDA(cudaEventRecordWithFlags(c->ev[3], c->stream, rflags));
     if (with_diag) {
         hc_diag_launch(c, c->d_diag);
@@ -795,6 +796,43 @@ static void drop_graphs(hc_ctx_ext *c)
             cudaGraphExecDestroy(g.exec);
             g.exec = nullptr;
         }
+}
+
+int hc_set_extpot(hc_ctx *ctx, const char *name, const double *par, int npar)
+{
+    if (!ctx || npar < 0 || (npar > 0 && !par)) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    const std::string nm = name ? name : "";
+    int kind = 0;
+    double p[4] = {1.0, 1.0, 1.0, 1.0};          // defaults of the plug-ins
+    if (nm.empty() || nm == "null") kind = 0;
+    else if (nm == "plummer") kind = HC_EXTPOT_PLUMMER;
+    else if (nm == "hernquist") kind = HC_EXTPOT_HERNQUIST;
+    else if (nm == "miyamoto") {
+        kind = HC_EXTPOT_MIYAMOTO;
+        p[1] = 0.0;                              // miyamoto.c: a = 0, b = 1
+    } else if (nm == "log") {
+        kind = HC_EXTPOT_LOG;
+    } else {
+        c->err = "hc_set_extpot: unknown potential '" + nm + "' (plummer, hernquist, miyamoto, log)";
+        return HC_ERR_ARG;
+    }
+    if (npar > 0 && par[0] != 0.0) {
+        c->err = "hc_set_extpot: a rotating frame (pattern speed != 0) is not supported";
+        return HC_ERR_ARG;
+    }
+    const int nmax = kind == HC_EXTPOT_LOG ? 5 : (kind == HC_EXTPOT_MIYAMOTO ? 4 : 3);
+    if (kind && npar > nmax) {
+        c->err = "hc_set_extpot: too many parameters for " + nm;
+        return HC_ERR_ARG;
+    }
+    for (int k = 1; k < npar; k++) p[k - 1] = par[k];
+    if (kind == HC_EXTPOT_LOG && npar <= 4) p[3] = p[2];      // log.c: r defaults to q
+    if (kind && !c->phi_ext) HC_TRY(dalloc(c, &c->phi_ext, c->n));
+    c->extpot = kind;
+    for (int k = 0; k < 4; k++) c->extpot_par[k] = p[k];
+    drop_graphs(c);
+    return HC_OK;
 }
 
 int hc_set_tuning(hc_ctx *ctx, const hc_tuning *t)

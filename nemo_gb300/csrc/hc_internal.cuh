@@ -133,6 +133,9 @@ struct hc_ctx {
     int64_t band_total;                   // band candidates seen by the last collection walk
     int criterion;                        // HC_CRITERION_* of include/hackcode_gpu.h
     float *rcrit2;                        // treecode1 criteria: critical radius^2 per node (lazy)
+    int extpot;                           // external potential (HC_EXTPOT_*), 0: none
+    double extpot_par[4];                 // its parameters after the pattern speed
+    double *phi_ext;                      // external potential per body (lazy)
     int group_max;                        // bodies per tree-aligned walk group (<= HC_GROUP)
     int list_depth;                       // interaction-list entries evaluated per flush (32..64)
     // forest of independent systems (hc_ensemble.cu): the walk of a group
@@ -198,6 +201,7 @@ int hc_relabel_impl(hc_ctx *c, float thr);
 // step (hc_step.cu)
 void hc_kick_drift(hc_ctx *c, double dt);
 void hc_diag_launch(hc_ctx *c, double *out36);
+void hc_extpot_launch(hc_ctx *c, double kick_dthf, int64_t nstep);
 void hc_direct_launch(hc_ctx *c, const int64_t *idx_dev, int64_t ns, double *oacc, double *ophi);
 void hc_rcrit_launch(hc_ctx *c, int kind, double theta);
 // guard (hc_guard.cu)

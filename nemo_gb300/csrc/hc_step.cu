@@ -33,6 +33,70 @@ __global__ void k_kick_drift(int64_t n, double dt, double *px, double *py, doubl
     }
 }
 
+// External potentials of NEMO's potential plug-ins (pattern speed 0),
+// restated: plummer (M, a) -M/sqrt(r^2 + a^2); hernquist (M, a) -M/(r + a);
+// miyamoto (M, a, b) -M/sqrt(R^2 + (a + sqrt(z^2 + b^2))^2); log (m_c, r_c,
+// q, r) (m_c/r_c) ln(r_c^2 + x^2 + y^2/q^2 + z^2/r^2).
+__device__ __forceinline__ void ext_field(int kind, const double *p, double x, double y, double z, double *ax,
+                                          double *ay, double *az, double *pot)
+{
+    if (kind == HC_EXTPOT_PLUMMER) {
+        const double t = 1.0 / (p[1] * p[1] + x * x + y * y + z * z), s = -sqrt(t);
+        *pot = p[0] * s;
+        const double f = t * s * p[0];
+        *ax = f * x;
+        *ay = f * y;
+        *az = f * z;
+    } else if (kind == HC_EXTPOT_HERNQUIST) {
+        const double r = sqrt(x * x + y * y + z * z), f = 1.0 / (r + p[1]);
+        *pot = -p[0] * f;
+        const double g = r > 0.0 ? -p[0] * f * f / r : 0.0;
+        *ax = g * x;
+        *ay = g * y;
+        *az = g * z;
+    } else if (kind == HC_EXTPOT_MIYAMOTO) {
+        const double q = sqrt(z * z + p[2] * p[2]), s = sqrt(x * x + y * y + (p[1] + q) * (p[1] + q));
+        *pot = -p[0] / s;
+        const double t = *pot / (s * s);
+        *ax = t * x;
+        *ay = t * y;
+        *az = t * z * (p[1] > 0.0 ? (p[1] + q) / q : 1.0);
+    } else {                                     // HC_EXTPOT_LOG
+        const double mor = p[1] > 0.0 ? p[0] / p[1] : p[0];
+        const double iq = 1.0 / (p[2] * p[2]), ir = 1.0 / (p[3] * p[3]);
+        const double rad = p[1] * p[1] + x * x + y * y * iq + z * z * ir;
+        *pot = mor * log(rad);
+        const double f = -2.0 * mor / rad;
+        *ax = f * x;
+        *ay = f * y * iq;
+        *az = f * z * ir;
+    }
+}
+
+// External field added to every body after the walk (hackcode3/grav.c:34-38),
+// and the rest of the closing half-kick: the walk kicked with the tree part
+// against the previous total acceleration.
+__global__ void k_extpot(int64_t n, int kind, double p0, double p1, double p2, double p3, const double *px,
+                         const double *py, const double *pz, double *ax, double *ay, double *az, double *phi,
+                         double *phi_ext, double *vx, double *vy, double *vz, double kick_dthf, int64_t nstep)
+{
+    const double p[4] = {p0, p1, p2, p3};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double fx, fy, fz, pot;
+        ext_field(kind, p, px[i], py[i], pz[i], &fx, &fy, &fz, &pot);
+        if (kick_dthf != 0.0 && nstep > 0) {
+            vx[i] = __dadd_rn(vx[i], __dmul_rn(fx, kick_dthf));
+            vy[i] = __dadd_rn(vy[i], __dmul_rn(fy, kick_dthf));
+            vz[i] = __dadd_rn(vz[i], __dmul_rn(fz, kick_dthf));
+        }
+        ax[i] = __dadd_rn(ax[i], fx);
+        ay[i] = __dadd_rn(ay[i], fy);
+        az[i] = __dadd_rn(az[i], fz);
+        phi[i] = __dadd_rn(phi[i], pot);
+        phi_ext[i] = pot;
+    }
+}
+
 __device__ __forceinline__ double wsum(double v)
 {
 #pragma unroll
@@ -45,7 +109,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_part(int64_t n, const dou
                                                             const double *py, const double *pz, const double *vx,
                                                             const double *vy, const double *vz, const double *ax,
                                                             const double *ay, const double *az, const double *phi,
-                                                            double *part)
+                                                            const double *phi_ext, double *part)
 {
     double acc[NDIAG];
 #pragma unroll
@@ -58,7 +122,9 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_part(int64_t n, const dou
         velsq = __dadd_rn(velsq, __dmul_rn(v[2], v[2]));
         const double hm = __dmul_rn(0.5, m);
         acc[0] += __dmul_rn(hm, velsq);
-        acc[1] += __dmul_rn(hm, phi[i]);
+        // with an external field phi holds tree + external; its energy
+        // counts the external part once more (hackcode3/code_io.c:180-186)
+        acc[1] += __dmul_rn(hm, phi_ext ? __dadd_rn(phi[i], phi_ext[i]) : phi[i]);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             const double tv = __dmul_rn(v[j], hm), tx = __dmul_rn(x[j], m);
@@ -195,13 +261,23 @@ void hc_kick_drift(hc_ctx *c, double dt)
     c->launches++;
 }
 
+void hc_extpot_launch(hc_ctx *c, double kick_dthf, int64_t nstep)
+{
+    const double *q = c->extpot_par;
+    k_extpot<<<hc_grid(c->n, 256), 256, 0, c->stream>>>(c->n, c->extpot, q[0], q[1], q[2], q[3], c->px, c->py, c->pz,
+                                                        c->ax, c->ay, c->az, c->phi, c->phi_ext, c->vx, c->vy, c->vz,
+                                                        kick_dthf, nstep);
+    c->launches++;
+}
+
 // out36 (device): KE, PE, keten, peten, amten(raw), sum m x, sum m v, mtot
 void hc_diag_launch(hc_ctx *c, double *out36)
 {
     int nb = (int)std::min<int64_t>(DIAG_BLOCKS, (c->n + DIAG_THREADS - 1) / DIAG_THREADS);
     if (nb < 1) nb = 1;
     k_diag_part<<<nb, DIAG_THREADS, 0, c->stream>>>(c->n, c->mass, c->px, c->py, c->pz, c->vx, c->vy, c->vz, c->ax,
-                                                    c->ay, c->az, c->phi, c->diag_part);
+                                                    c->ay, c->az, c->phi, c->extpot ? c->phi_ext : nullptr,
+                                                    c->diag_part);
     k_diag_final<<<1, 64, 0, c->stream>>>(c->diag_part, nb, out36);
     c->launches += 2;
 }

@@ -33,7 +33,7 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
            "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band", "hc_set_guard", "hc_guard_stats",
            "hc_ens_create", "hc_ens_destroy", "hc_ens_last_error", "hc_ens_upload", "hc_ens_step",
-           "hc_ens_download", "hc_ens_info", "hc_set_tuning", "hc_get_tuning", "hc_autotune"]
+           "hc_ens_download", "hc_ens_info", "hc_set_tuning", "hc_get_tuning", "hc_autotune", "hc_set_extpot"]
 
 
 class HCError(RuntimeError):
@@ -127,6 +127,7 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_set_grouping.argtypes = [_vp, C.c_int]
     L.hc_set_guard.argtypes = [_vp, C.c_int64, C.c_double, C.c_uint64]
     L.hc_set_tuning.argtypes = [_vp, C.POINTER(Tuning)]
+    L.hc_set_extpot.argtypes = [_vp, C.c_char_p, _vp, C.c_int]
     L.hc_get_tuning.argtypes = [_vp, C.POINTER(Tuning)]
     L.hc_autotune.argtypes = [_vp, C.POINTER(Tuning)]
     L.hc_ens_create.argtypes = [C.POINTER(_vp), C.c_int, _lp, C.POINTER(EnsParams)]
@@ -315,6 +316,12 @@ class Context:
     def set_grouping(self, kind: str = "consecutive"):
         """Walk groups: 'consecutive' (32 bodies in key order) or 'tree' (cells of <= 32 bodies)."""
         self._check(self._L.hc_set_grouping(self._h, {"consecutive": 0, "tree": 1}[kind]))
+
+    def set_extpot(self, name=None, pars=()):
+        """External potential (hackcode3's potname= / potpars=): 'plummer', 'hernquist',
+        'miyamoto' or 'log' with NEMO's parameter order (pattern speed first, must be 0)."""
+        p = np.ascontiguousarray(pars, dtype=np.float64)
+        self._check(self._L.hc_set_extpot(self._h, (name or "").encode(), _ptr(p) if len(p) else None, len(p)))
 
     def set_tuning(self, group_max=32, list_depth=64, grouping="consecutive"):
         t = Tuning(int(group_max), int(list_depth), {"consecutive": 0, "tree": 1}[grouping], 0.0)
