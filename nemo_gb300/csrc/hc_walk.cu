@@ -558,17 +558,20 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
                 }
             }
             if (MODE == 3) {                   // enqueue band candidates
+                // (the warp syncs at the end of this iteration order these
+                // writes before the round that reads them)
                 const unsigned qb = __ballot_sync(FULL, band);
-                if (band) {
-                    const int row = qn + __popc(qb & lt);
-                    Qs->node[row] = my_node;
-                    Qs->mask[row] = my_mask;
-                    Qs->dmin2[row] = bd_dmin2;
-                    Qs->dmax2[row] = bd_dmax2;
-                    Qs->err[row] = bd_err;
+                if (qb) {
+                    if (band) {
+                        const int row = qn + __popc(qb & lt);
+                        Qs->node[row] = my_node;
+                        Qs->mask[row] = my_mask;
+                        Qs->dmin2[row] = bd_dmin2;
+                        Qs->dmax2[row] = bd_dmax2;
+                        Qs->err[row] = bd_err;
+                    }
+                    qn += __popc(qb);
                 }
-                qn += __popc(qb);
-                __syncwarp();
             }
             unsigned mixedb = MODE == 0 ? __ballot_sync(FULL, mixed) : 0u;
             if (lane == 0) {
