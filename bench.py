@@ -576,12 +576,24 @@ def run_galaxy(args, world, rank, local):
     if not torch.cuda.is_available():
         raise SystemExit("bench.py: no CUDA device (the CUDA path has no CPU fallback)")
     torch.cuda.set_device(local)
-    t0 = time.perf_counter()
-    m, ph = hc.mkgalaxy(*GAL_N, seed=GAL_SEED)
-    t_gen = time.perf_counter() - t0
-    n = len(m)
+    n = sum(GAL_N)
     ctx = hc.Context(n, tol=TOL, eps=GAL_EPS, fcells=1.0, usequad=USEQUAD)
-    ctx.upload(m, ph)
+    if args.generator == "host":
+        t0 = time.perf_counter()
+        m, ph = hc.mkgalaxy(*GAL_N, seed=GAL_SEED)
+        t_gen = time.perf_counter() - t0
+
+    def initial_conditions():
+        if args.generator == "host":
+            ctx.upload(m, ph)
+        else:
+            ctx.generate("galaxy", GAL_SEED, list(GAL_N[:2]))
+
+    if args.generator == "device":
+        t0 = time.perf_counter()
+        initial_conditions()
+        t_gen = time.perf_counter() - t0
+    initial_conditions()
     ctx.evaluate()
     rng = np.random.default_rng(12345)
     idx = np.sort(rng.choice(n, size=min(args.sample, 4096), replace=False)).astype(np.int64)
@@ -595,7 +607,7 @@ def run_galaxy(args, world, rank, local):
     set_mode(ctx, mode)
     ctx.set_guard(GUARD_SAMPLE, RMS_BUDGET, seed=1)
     # start the run from the initial conditions
-    ctx.upload(m, ph)
+    initial_conditions()
     d0, _, _, _ = ctx.step(GAL_DT, 0)
     e0, l0 = d0.etot[0], angular_momentum(d0)
     for k in range(1, args.warmup + 1):
@@ -615,7 +627,8 @@ def run_galaxy(args, world, rank, local):
         "metric": "composite galaxy leapfrog body-steps/s", "value": world * n / (mean_ms * 1e-3),
         "unit": "body-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: composite disk galaxy (project generator, ran3 seed=11)",
+        "data": "synthetic: composite disk galaxy (project generator, " +
+                ("ran3 seed=11)" if args.generator == "host" else "device counter-based streams, seed=11)"),
         "config": {"workload": f"disk {GAL_N[0]} + Hernquist bulge {GAL_N[1]} + NFW halo {GAL_N[2]} bodies, "
                                f"eps={GAL_EPS}, dt=1/512, quadrupole, learned criterion (guarded), one CUDA graph "
                                f"per step", "criterion_setting": list(mode),
@@ -626,7 +639,8 @@ def run_galaxy(args, world, rank, local):
         "rms_error": {"learned": lrn_pt["rms"] if lrn_pt else None, "fixed_theta_0.5": fixed["rms"],
                       "sample": int(len(idx))},
         "evaluation_ms": {"learned": lrn_pt["step_ms"] if lrn_pt else None, "fixed_theta_0.5": fixed["step_ms"]},
-        "calibration": cal, "training": train, "guard": guard, "generator_seconds": t_gen,
+        "calibration": cal, "training": train, "guard": guard,
+        "generator": {"where": args.generator, "seconds": t_gen},
         "clocks": clk.summary(),
     }
     ctx.close()
@@ -679,6 +693,8 @@ def main():
                     help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
                          "ensemble: 4096 independent systems; galaxy: 2^24-body disk galaxy, leapfrog")
     ap.add_argument("--nsys", type=int, default=ENS_NSYS)
+    ap.add_argument("--generator", default="host", choices=["host", "device"],
+                    help="galaxy workload: draw the bodies with mkgalaxy on the host or hc_generate on the device")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -308,6 +308,20 @@ void hc_mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase)
  * the order disk, bulge, halo; ran3 seeded with seed. */
 void hc_mkgalaxy(int64_t n_disk, int64_t n_bulge, int64_t n_halo, int seed, double *mass, double *phase);
 
+/* Initial conditions drawn on the device straight into the context's bodies
+ * (replaces hc_upload; forces and potentials are zeroed).  model "plummer":
+ * mkplummer's model and sampling steps (src/nbody/init/mkplummer.c:257-422),
+ * par[0] = mfrac (default 0.999, capped at the mass inside rfrac); model
+ * "hernquist": hc_mkhernquist's model, par[0] = rtrunc (default 100); model
+ * "galaxy": hc_mkgalaxy's model with its tables and per-body steps, par[0] =
+ * n_disk (default n/4), par[1] = n_bulge (default n/16), the rest halo.  Every
+ * body draws from its own counter-based stream of seed, so the sample is
+ * another draw of the same model than the host generators give, equal for
+ * equal (n, seed) on every device.  Centre of mass and its velocity are
+ * removed.  HC_ERR_ARG for an unknown model or bad parameters; HC_ERR_STATE
+ * if a velocity rejection loop hit its iteration limit. */
+int hc_generate(hc_ctx *ctx, const char *model, uint64_t seed, const double *par, int npar);
+
 /* Host services of the drop-in programs, exported for tests: copy every
  * snapshot of a filestruct file through the reader and writer (returns the
  * snapshot count or -1), and evaluate a keyword expression as getdparam does

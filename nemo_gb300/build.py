@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhackcode_gpu.so")
 
-CU_SOURCES = ["hc_sort.cu", "hc_tree.cu", "hc_walk.cu", "hc_step.cu", "hc_api.cu", "hc_noalloc.cu", "hc_learn.cu", "hc_guard.cu", "hc_ensemble.cu"]
+CU_SOURCES = ["hc_sort.cu", "hc_tree.cu", "hc_walk.cu", "hc_step.cu", "hc_api.cu", "hc_noalloc.cu", "hc_learn.cu", "hc_guard.cu", "hc_ensemble.cu", "hc_gen.cu"]
 HOST_LIB_SOURCES = ["nemo_io.cpp", "galaxy.cpp"]
 PROGRAMS = {"hackcode1": "hackcode1_main.cpp", "hackforce": "hackforce_main.cpp"}
 

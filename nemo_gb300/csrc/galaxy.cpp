@@ -27,19 +27,16 @@
 // Bodies: disk, then bulge, then halo; equal masses within each component;
 // the centre of mass and its velocity are removed at the end.
 #include <algorithm>
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <vector>
+#include "galaxy_model.h"
 #include "nemo_io.h"
 
-namespace nemo {
+namespace galaxy {
 
 namespace {
-
-constexpr double PI = 3.141592653589793238462643;
-constexpr double MD = 0.1, RD = 1.0, Z0 = 0.1, QT = 1.5, RDMAX = 15.0;
-constexpr double MB = 0.033, AB = 0.2;
-constexpr double MV = 1.0, RV = 30.0, CC = 10.0, RS = RV / CC;
 
 double nfw_m(double x) { return std::log1p(x) - x / (1.0 + x); }
 
@@ -68,61 +65,27 @@ double m_disk_sph(double r)
     return MD * (1.0 - (1.0 + x) * std::exp(-x)) / (1.0 - (1.0 + RDMAX) * std::exp(-RDMAX));
 }
 
-struct Grid {
-    std::vector<double> r, psi;          // psi decreasing with r
-    double mtot = 0.0;
-    double psi_at(double x) const
-    {
-        if (x <= r.front()) return psi.front();
-        if (x >= r.back()) return mtot / x;
-        const double lx = std::log(x), l0 = std::log(r.front()), l1 = std::log(r.back());
-        const double t = (lx - l0) / (l1 - l0) * (double)(r.size() - 1);
-        const size_t i = std::min((size_t)t, r.size() - 2);
-        const double w = t - (double)i;
-        return psi[i] * (1.0 - w) + psi[i + 1] * w;
-    }
-};
-
-Grid make_grid()
+// psi(r) = int_r^inf M(r') / r'^2 dr' = int M / r d ln r, from the outside in
+void make_grid(Tables &g)
 {
-    Grid g;
-    const int K = 4000;
+    const int K = KG;
     const double l0 = std::log(1e-6), l1 = std::log(1e4);
     g.r.resize(K);
     g.psi.resize(K);
     for (int i = 0; i < K; i++) g.r[i] = std::exp(l0 + (l1 - l0) * i / (K - 1));
     auto mt = [](double r) { return m_bulge(r) + m_halo(r) + m_disk_sph(r); };
     g.mtot = mt(1e9);
-    // psi(r) = int_r^inf M(r') / r'^2 dr' = int M / r d ln r, from the outside in
     g.psi[K - 1] = g.mtot / g.r[K - 1];
     for (int i = K - 2; i >= 0; i--) {
         const double dl = std::log(g.r[i + 1]) - std::log(g.r[i]);
         g.psi[i] = g.psi[i + 1] + 0.5 * dl * (mt(g.r[i]) / g.r[i] + mt(g.r[i + 1]) / g.r[i + 1]);
     }
-    return g;
 }
 
 // Isotropic distribution function of one spherical component in the total
-// potential, tabulated against E = psi(r_j).
-struct DF {
-    std::vector<double> E, f;            // E decreasing
-    double at(double e) const
-    {
-        if (e <= E.back()) return 0.0;
-        if (e >= E.front()) return f.front();
-        // E is decreasing: binary search
-        size_t lo = 0, hi = E.size() - 1;
-        while (hi - lo > 1) {
-            const size_t mid = (lo + hi) / 2;
-            if (E[mid] > e) lo = mid;
-            else hi = mid;
-        }
-        const double w = (e - E[hi]) / (E[lo] - E[hi]);
-        return f[hi] + w * (f[lo] - f[hi]);
-    }
-};
-
-DF eddington(const Grid &g, double (*rho)(double))
+// potential, tabulated against E = psi(r_j) (Eddington's inversion).
+void eddington(const Tables &g, const View &gv, double (*rho)(double), std::vector<double> &E,
+               std::vector<double> &f)
 {
     const size_t K = g.r.size();
     std::vector<double> dr(K, 0.0);      // drho/dpsi at grid points
@@ -142,14 +105,13 @@ DF eddington(const Grid &g, double (*rho)(double))
         return dr[hi] + w * (dr[lo] - dr[hi]);
     };
     // G(E) = int_0^sqrt(E) 2 drho/dpsi(E - t^2) dt  (t = sqrt(E - psi))
-    const int J = 1200, T = 400;
-    DF d;
-    d.E.resize(J);
+    const int J = JE, T = 400;
+    E.resize(J);
     std::vector<double> G(J);
-    const double e0 = g.psi.front(), e1 = g.psi_at(RV * 1.5);
+    const double e0 = g.psi.front(), e1 = psi_at(gv, RV * 1.5);
     for (int j = 0; j < J; j++) {
         const double e = std::exp(std::log(e0) + (std::log(e1) - std::log(e0)) * j / (J - 1));
-        d.E[j] = e;
+        E[j] = e;
         const double tmax = std::sqrt(e);
         double s = 0.0;
         for (int k = 0; k < T; k++) {
@@ -158,154 +120,139 @@ DF eddington(const Grid &g, double (*rho)(double))
         }
         G[j] = s * tmax / T;
     }
-    d.f.resize(J);
+    f.resize(J);
     const double norm = 1.0 / (std::sqrt(8.0) * PI * PI);
     for (int j = 0; j < J; j++) {
         const int a = j == 0 ? 0 : j - 1, b = j == J - 1 ? J - 1 : j + 1;
-        const double v = (G[a] - G[b]) / (d.E[a] - d.E[b]) * norm;
-        d.f[j] = v > 0.0 ? v : 0.0;
+        const double v = (G[a] - G[b]) / (E[a] - E[b]) * norm;
+        f[j] = v > 0.0 ? v : 0.0;
     }
-    return d;
-}
-
-double gauss(Ran3 &r)
-{
-    // Box-Muller on ran3 uniforms
-    const double u1 = r.uniform(1e-300, 1.0), u2 = r.uniform(0.0, 2.0 * PI);
-    return std::sqrt(-2.0 * std::log(u1)) * std::cos(u2);
-}
-
-void iso_direction(Ran3 &r, double len, double *v)
-{
-    const double ct = r.uniform(-1.0, 1.0), st = std::sqrt(std::max(0.0, 1.0 - ct * ct));
-    const double ph = r.uniform(0.0, 2.0 * PI);
-    v[0] = len * st * std::cos(ph);
-    v[1] = len * st * std::sin(ph);
-    v[2] = len * ct;
 }
 
 // max over v of g(v) = v^2 f(psi - v^2/2) (grid on v = vmax t^2, fine near 0)
-double gmax_at(const DF &df, double psi)
+double gmax_at(const double *E, const double *f, double psi)
 {
     const double vmax = std::sqrt(2.0 * psi);
     double m = 0.0;
     const int K = 128;
     for (int k = 1; k < K; k++) {
         const double t = (double)k / K, v = vmax * t * t;
-        m = std::max(m, v * v * df.at(psi - 0.5 * v * v));
+        m = std::max(m, v * v * df_at(E, f, psi - 0.5 * v * v));
     }
     return m;
 }
 
-// speed at radius r from g(v), by rejection under bound
-double sample_speed(Ran3 &r, const DF &df, double psi, double bound)
-{
-    const double vmax = std::sqrt(2.0 * psi);
-    if (!(bound > 0.0)) return 0.0;
-    for (int tries = 0; tries < 1000000; tries++) {
-        const double v = r.uniform(0.0, vmax);
-        if (r.uniform(0.0, bound) <= v * v * df.at(psi - 0.5 * v * v)) return v;
-    }
-    return 0.0;
-}
-
-// radius from a tabulated cumulative mass (monotone), by interpolation
-double invert(const std::vector<double> &rr, const std::vector<double> &mm, double u)
-{
-    const size_t i = std::upper_bound(mm.begin(), mm.end(), u) - mm.begin();
-    if (i == 0) return rr.front();
-    if (i >= mm.size()) return rr.back();
-    const double w = (u - mm[i - 1]) / (mm[i] - mm[i - 1]);
-    return rr[i - 1] + w * (rr[i] - rr[i - 1]);
-}
+struct HostDraw {
+    nemo::Ran3 &r;
+    double operator()(double lo, double hi) { return r.uniform(lo, hi); }
+};
 
 }  // namespace
 
+View Tables::view() const
+{
+    View v{};
+    v.r = r.data();
+    v.psi = psi.data();
+    v.mtot = mtot;
+    v.lr0 = r.empty() ? 0.0 : std::log(r.front());
+    v.lr1 = r.empty() ? 0.0 : std::log(r.back());
+    v.xr = xr.data();
+    v.xm = xm.data();
+    v.tsr = tsr.data();
+    v.tsphi = tsphi.data();
+    v.tsz = tsz.data();
+    v.tvphi = tvphi.data();
+    for (int c = 0; c < 2; c++) {
+        v.dfE[c] = dfE[c].data();
+        v.dff[c] = dff[c].data();
+        v.rr[c] = rr[c].data();
+        v.mm[c] = mm[c].data();
+        v.bnd[c] = bnd[c].data();
+        v.mcomp[c] = mcomp[c];
+    }
+    return v;
+}
+
+void build_tables(Tables &t)
+{
+    make_grid(t);
+    const View gv = t.view();
+    // ---- disk: cumulative mass of the truncated exponential, kinematics
+    const double sigma0 = MD / (2.0 * PI * RD * RD) / (1.0 - (1.0 + RDMAX) * std::exp(-RDMAX));
+    t.xr.resize(NX);
+    t.xm.resize(NX);
+    for (int k = 0; k < NX; k++) {
+        const double x = RDMAX * k / (NX - 1.0);
+        t.xr[k] = x;
+        t.xm[k] = (1.0 - (1.0 + x) * std::exp(-x)) / (1.0 - (1.0 + RDMAX) * std::exp(-RDMAX));
+    }
+    auto vc2 = [&](double R) {
+        const double y = std::max(R, 1e-8) / (2.0 * RD);
+        const double vd2 = 4.0 * PI * sigma0 * RD * y * y *
+                           (std::cyl_bessel_i(0.0, y) * std::cyl_bessel_k(0.0, y) -
+                            std::cyl_bessel_i(1.0, y) * std::cyl_bessel_k(1.0, y));
+        return vd2 + (m_bulge(R) + m_halo(R)) / std::max(R, 1e-8);
+    };
+    // kinematics on a radius grid (kappa from a centred difference of R^2 vc^2)
+    t.tsr.resize(KR);
+    t.tsphi.resize(KR);
+    t.tsz.resize(KR);
+    t.tvphi.resize(KR);
+    for (int k = 0; k < KR; k++) {
+        const double R = std::max(RD * RDMAX * k / (KR - 1.0), 1e-4);
+        const double h = 1e-3 * R;
+        const double v2 = vc2(R), om2 = v2 / (R * R);
+        const double L2p = (R + h) * (R + h) * vc2(R + h), L2m = (R - h) * (R - h) * vc2(R - h);
+        const double kappa2 = std::max((L2p - L2m) / (2.0 * h) / (R * R * R), 1e-12);
+        const double sig = sigma0 * std::exp(-R / RD);
+        t.tsr[k] = QT * 3.36 * sig / std::sqrt(kappa2);
+        t.tsphi[k] = t.tsr[k] * std::sqrt(kappa2 / (4.0 * om2));
+        t.tsz[k] = std::sqrt(PI * sig * Z0);
+        t.tvphi[k] = std::sqrt(std::max(v2 + t.tsr[k] * t.tsr[k] * (1.0 - kappa2 / (4.0 * om2) - 2.0 * R / RD), 0.0));
+    }
+    // ---- bulge and halo: distribution functions, mass inversion, bounds
+    double (*rho[2])(double) = {rho_bulge, rho_halo};
+    double (*mfun[2])(double) = {m_bulge, m_halo};
+    for (int c = 0; c < 2; c++) {
+        eddington(t, gv, rho[c], t.dfE[c], t.dff[c]);
+        t.rr[c].resize(NX);
+        t.mm[c].resize(NX);
+        for (int k = 0; k < NX; k++) {
+            t.rr[c][k] = std::exp(std::log(1e-6) + (std::log(RV) - std::log(1e-6)) * k / (NX - 1.0));
+            t.mm[c][k] = mfun[c](t.rr[c][k]) / t.mcomp[c];
+        }
+        // rejection bound per radius: sampled with the larger grid neighbour and a 25% margin
+        t.bnd[c].resize(KB);
+        const double lb0 = std::log(1e-6), lb1 = std::log(RV);
+        for (int k = 0; k < KB; k++)
+            t.bnd[c][k] = gmax_at(t.dfE[c].data(), t.dff[c].data(), psi_at(gv, std::exp(lb0 + (lb1 - lb0) * k / (KB - 1.0))));
+    }
+}
+
+}  // namespace galaxy
+
+namespace nemo {
+
 void mkgalaxy(int64_t nd, int64_t nb, int64_t nh, int seed, double *mass, double *phase)
 {
+    using namespace galaxy;
     Ran3 r(seed);
-    const Grid g = make_grid();
-    // ---- disk ----
-    {
-        const double sigma0 = MD / (2.0 * PI * RD * RD) / (1.0 - (1.0 + RDMAX) * std::exp(-RDMAX));
-        std::vector<double> xr(8192), xm(8192);
-        for (int k = 0; k < 8192; k++) {
-            const double x = RDMAX * k / 8191.0;
-            xr[k] = x;
-            xm[k] = (1.0 - (1.0 + x) * std::exp(-x)) / (1.0 - (1.0 + RDMAX) * std::exp(-RDMAX));
-        }
-        auto vc2 = [&](double R) {
-            const double y = std::max(R, 1e-8) / (2.0 * RD);
-            const double vd2 = 4.0 * PI * sigma0 * RD * y * y *
-                               (std::cyl_bessel_i(0.0, y) * std::cyl_bessel_k(0.0, y) -
-                                std::cyl_bessel_i(1.0, y) * std::cyl_bessel_k(1.0, y));
-            return vd2 + (m_bulge(R) + m_halo(R)) / std::max(R, 1e-8);
-        };
-        // kinematics on a radius grid (kappa from a centred difference of R^2 vc^2)
-        const int KR = 4096;
-        std::vector<double> tsr(KR), tsphi(KR), tsz(KR), tvphi(KR);
-        for (int k = 0; k < KR; k++) {
-            const double R = std::max(RD * RDMAX * k / (KR - 1.0), 1e-4);
-            const double h = 1e-3 * R;
-            const double v2 = vc2(R), om2 = v2 / (R * R);
-            const double L2p = (R + h) * (R + h) * vc2(R + h), L2m = (R - h) * (R - h) * vc2(R - h);
-            const double kappa2 = std::max((L2p - L2m) / (2.0 * h) / (R * R * R), 1e-12);
-            const double sig = sigma0 * std::exp(-R / RD);
-            tsr[k] = QT * 3.36 * sig / std::sqrt(kappa2);
-            tsphi[k] = tsr[k] * std::sqrt(kappa2 / (4.0 * om2));
-            tsz[k] = std::sqrt(PI * sig * Z0);
-            tvphi[k] = std::sqrt(std::max(v2 + tsr[k] * tsr[k] * (1.0 - kappa2 / (4.0 * om2) - 2.0 * R / RD), 0.0));
-        }
-        auto lerp = [&](const std::vector<double> &t, double R) {
-            const double x = R / (RD * RDMAX) * (KR - 1.0);
-            const int k = std::min((int)x, KR - 2);
-            const double w = x - k;
-            return t[k] * (1.0 - w) + t[k + 1] * w;
-        };
-        for (int64_t i = 0; i < nd; i++) {
-            double *p = phase + 6 * i, *v = p + 3;
-            mass[i] = MD / (double)nd;
-            const double R = RD * invert(xr, xm, r.uniform(0.0, 1.0));
-            const double ph = r.uniform(0.0, 2.0 * PI);
-            double u = r.uniform(-1.0, 1.0);
-            u = std::max(-1.0 + 1e-12, std::min(1.0 - 1e-12, u));
-            p[0] = R * std::cos(ph);
-            p[1] = R * std::sin(ph);
-            p[2] = Z0 * std::atanh(u);
-            const double sr = lerp(tsr, R), sphi = lerp(tsphi, R), sz = lerp(tsz, R);
-            const double vphi = lerp(tvphi, R) + sphi * gauss(r);
-            const double vr = sr * gauss(r), vz = sz * gauss(r);
-            v[0] = vr * std::cos(ph) - vphi * std::sin(ph);
-            v[1] = vr * std::sin(ph) + vphi * std::cos(ph);
-            v[2] = vz;
-        }
+    HostDraw u{r};
+    Tables tab;
+    build_tables(tab);
+    const View t = tab.view();
+    bool fail = false;
+    for (int64_t i = 0; i < nd; i++) {
+        mass[i] = MD / (double)nd;
+        disk_body(t, u, phase + 6 * i, phase + 6 * i + 3);
     }
-    // ---- spherical components ----
-    auto spherical = [&](int64_t off, int64_t n, double mtot, double (*mfun)(double), double (*rho)(double)) {
-        const DF df = eddington(g, rho);
-        std::vector<double> rr(8192), mm(8192);
-        for (int k = 0; k < 8192; k++) {
-            rr[k] = std::exp(std::log(1e-6) + (std::log(RV) - std::log(1e-6)) * k / 8191.0);
-            mm[k] = mfun(rr[k]) / mtot;
+    const int64_t off[2] = {nd, nd + nb}, cnt[2] = {nb, nh};
+    for (int c = 0; c < 2; c++)
+        for (int64_t i = off[c]; i < off[c] + cnt[c]; i++) {
+            mass[i] = t.mcomp[c] / (double)cnt[c];
+            sphere_body(t, c, u, phase + 6 * i, phase + 6 * i + 3, &fail);
         }
-        // rejection bound per radius: the larger neighbour on the grid, 25% margin
-        const int KB = 2048;
-        std::vector<double> bnd(KB);
-        const double lb0 = std::log(1e-6), lb1 = std::log(RV);
-        for (int k = 0; k < KB; k++) bnd[k] = gmax_at(df, g.psi_at(std::exp(lb0 + (lb1 - lb0) * k / (KB - 1.0))));
-        for (int64_t i = off; i < off + n; i++) {
-            double *p = phase + 6 * i, *v = p + 3;
-            mass[i] = mtot / (double)n;
-            const double rad = invert(rr, mm, r.uniform(0.0, 1.0));
-            iso_direction(r, rad, p);
-            const double x = (std::log(std::max(rad, 1e-6)) - lb0) / (lb1 - lb0) * (KB - 1.0);
-            const int k = std::max(0, std::min((int)x, KB - 2));
-            const double psi = g.psi_at(rad);
-            iso_direction(r, sample_speed(r, df, psi, 1.25 * std::max(bnd[k], bnd[k + 1])), v);
-        }
-    };
-    spherical(nd, nb, MB, m_bulge, rho_bulge);
-    spherical(nd + nb, nh, MV, m_halo, rho_halo);
     // ---- centre of mass at rest at the origin ----
     const int64_t n = nd + nb + nh;
     double mt = 0.0, cp[3] = {0, 0, 0}, cv[3] = {0, 0, 0};

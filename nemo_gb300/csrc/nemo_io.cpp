@@ -212,6 +212,13 @@ static double hernquist_gmax(double psi)
     return std::max(best, g(0.5 * (lo + hi)));
 }
 
+void hernquist_gmax_table(double rtrunc, int T, double *tab, double *lr0, double *lr1)
+{
+    *lr0 = std::log(1e-7);
+    *lr1 = std::log(rtrunc * 1.01);
+    for (int k = 0; k < T; k++) tab[k] = hernquist_gmax(1.0 / (1.0 + std::exp(*lr0 + (*lr1 - *lr0) * k / (T - 1))));
+}
+
 void mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase)
 {
     const double two_pi = 6.283185307179586476925287;
@@ -220,9 +227,9 @@ void mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase)
     // bound table on log-spaced radii: gmax is smooth in r; use the larger
     // neighbour and a 10% margin
     const int T = 2048;
-    const double lr0 = std::log(1e-7), lr1 = std::log(rtrunc * 1.01);
+    double lr0 = 0.0, lr1 = 0.0;
     std::vector<double> tab(T);
-    for (int k = 0; k < T; k++) tab[k] = hernquist_gmax(1.0 / (1.0 + std::exp(lr0 + (lr1 - lr0) * k / (T - 1))));
+    hernquist_gmax_table(rtrunc, T, tab.data(), &lr0, &lr1);
     for (int i = 0; i < n; i++) {
         double *p = phase + 6 * i, *v = p + 3;
         mass[i] = mt / (double)n;

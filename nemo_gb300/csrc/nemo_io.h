@@ -29,6 +29,9 @@ void mkplummer(int n, int seed, double *mass, double *phase);
 // isotropic Hernquist sphere (G = M = a = 1) truncated at rtrunc; velocities
 // from the Eddington-inverted distribution function (project-written)
 void mkhernquist(int n, int seed, double rtrunc, double *mass, double *phase);
+// the rejection bound mkhernquist uses: max over v of v^2 f(psi(r) - v^2/2)
+// on T radii log-spaced in [exp(lr0), exp(lr1)]
+void hernquist_gmax_table(double rtrunc, int T, double *tab, double *lr0, double *lr1);
 
 // ---- filestruct (src/kernel/io/filesecret.c, inc/filestruct.h)
 struct Item {

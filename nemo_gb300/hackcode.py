@@ -33,7 +33,8 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
            "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band", "hc_set_guard", "hc_guard_stats",
            "hc_ens_create", "hc_ens_destroy", "hc_ens_last_error", "hc_ens_upload", "hc_ens_step",
-           "hc_ens_download", "hc_ens_info", "hc_set_tuning", "hc_get_tuning", "hc_autotune", "hc_set_extpot"]
+           "hc_ens_download", "hc_ens_info", "hc_set_tuning", "hc_get_tuning", "hc_autotune", "hc_set_extpot",
+           "hc_generate"]
 
 
 class HCError(RuntimeError):
@@ -128,6 +129,7 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_set_guard.argtypes = [_vp, C.c_int64, C.c_double, C.c_uint64]
     L.hc_set_tuning.argtypes = [_vp, C.POINTER(Tuning)]
     L.hc_set_extpot.argtypes = [_vp, C.c_char_p, _vp, C.c_int]
+    L.hc_generate.argtypes = [_vp, C.c_char_p, C.c_uint64, _vp, C.c_int]
     L.hc_get_tuning.argtypes = [_vp, C.POINTER(Tuning)]
     L.hc_autotune.argtypes = [_vp, C.POINTER(Tuning)]
     L.hc_ens_create.argtypes = [C.POINTER(_vp), C.c_int, _lp, C.POINTER(EnsParams)]
@@ -243,6 +245,12 @@ class Context:
         raw = self._L["hc_upload"]          # a second handle with pointer-typed arguments
         raw.argtypes = [_vp, _vp, _vp]
         self._check(raw(self._h, mass_ptr, phase_ptr))
+
+    def generate(self, model="plummer", seed=1, pars=()):
+        """Draw initial conditions on the device (hc_generate): 'plummer' (pars: mfrac),
+        'hernquist' (pars: rtrunc) or 'galaxy' (pars: n_disk, n_bulge; the rest is halo)."""
+        p = np.ascontiguousarray(pars, dtype=np.float64)
+        self._check(self._L.hc_generate(self._h, model.encode(), int(seed), _ptr(p) if len(p) else None, len(p)))
 
     def set_forces(self, acc=None, phi=None):
         """Accelerations [n][3] / potentials [n] of a previous evaluation (restart state)."""
