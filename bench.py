@@ -214,7 +214,7 @@ LEARNED_THRESHOLD = 0.0      # logit threshold of the learned criterion (0: the 
 BISECT_STEPS = 7
 
 
-TUNING = {"body": None, "group": {"group_max": 32, "list_depth": 64, "grouping": "tree"}}
+TUNING = {"body": None, "group": {"group_max": 64, "list_depth": 64, "grouping": "tree"}}
 
 
 def set_mode(ctx, mode):
@@ -222,7 +222,7 @@ def set_mode(ctx, mode):
     The context's tol is theta for the per-body rule and 0.5 otherwise (the
     fallback of the guard).  The per-body rule runs with the autotuner's
     choice (its interaction sets do not depend on it); the group criteria with
-    32-body tree groups."""
+    tree groups of up to 64 bodies (two per lane)."""
     t = TUNING["body"] if mode[0] == "body" and TUNING["body"] else TUNING["group"]
     ctx.set_tuning(t["group_max"], t["list_depth"], t["grouping"])
     if mode[0] == "body":

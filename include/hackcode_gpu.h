@@ -251,12 +251,14 @@ enum { HC_EXTPOT_PLUMMER = 1, HC_EXTPOT_HERNQUIST = 2, HC_EXTPOT_MIYAMOTO = 3, H
 int hc_set_extpot(hc_ctx *ctx, const char *name, const double *par, int npar);
 
 /* Walk tuning (no counterpart in hackcode1): the largest walk group of tree
- * grouping (1..32 bodies per warp), the interaction-list depth evaluated per
- * flush (32..64 entries) and the grouping kind.  hc_autotune times one
- * evaluation of the bodies and criterion currently set for each candidate
- * (group_max 16/24/32 x list_depth 32/48/64 on tree groups, plus consecutive
- * groups for the per-body rule), keeps the fastest and returns it with its
- * time in ms.  With the per-body rule the interaction sets do not depend on
+ * grouping (1..64 bodies per warp; the per-body rule, one body per lane, uses
+ * at most 32, the group criteria two bodies per lane), the interaction-list
+ * depth evaluated per flush (32..64 entries) and the grouping kind (the group
+ * criteria always walk tree groups).  hc_autotune times one evaluation of the
+ * bodies and criterion currently set for each candidate (group_max 16/24/32
+ * for the per-body rule, 32/48/64 for the group criteria, x list_depth
+ * 32/48/64 on tree groups, plus consecutive groups for the per-body rule),
+ * keeps the fastest and returns it with its time in ms.  With the per-body rule the interaction sets do not depend on
  * the tuning; with the approximate criteria the group size changes which
  * cells are accepted. */
 typedef struct {

@@ -267,7 +267,7 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
     c->maxnode = nbody + c->maxcell;
     c->mlp_band = 1.0f;
     c->mlp_band_hi = 3.0f;
-    c->group_max = HC_GROUP;
+    c->group_max = HC_GROUP2;
     c->list_depth = 64;
     *out = c;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -839,9 +839,9 @@ int hc_set_tuning(hc_ctx *ctx, const hc_tuning *t)
 {
     if (!ctx || !t) return HC_ERR_ARG;
     hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
-    if (t->group_max < 1 || t->group_max > HC_GROUP || t->list_depth < 32 || t->list_depth > 64 ||
+    if (t->group_max < 1 || t->group_max > HC_GROUP2 || t->list_depth < 32 || t->list_depth > 64 ||
         (t->grouping != HC_GROUPS_CONSECUTIVE && t->grouping != HC_GROUPS_TREE)) {
-        c->err = "hc_set_tuning: group_max 1..32, list_depth 32..64, grouping HC_GROUPS_*";
+        c->err = "hc_set_tuning: group_max 1..64, list_depth 32..64, grouping HC_GROUPS_*";
         return HC_ERR_ARG;
     }
     c->group_max = t->group_max;
@@ -868,8 +868,10 @@ int hc_autotune(hc_ctx *ctx, hc_tuning *best)
     hc_tuning keep;
     hc_get_tuning(ctx, &keep);
     std::vector<hc_tuning> cand;
-    const int gms[] = {16, 24, 32}, lds[] = {32, 48, 64};
-    for (int gm : gms)
+    // the per-body rule walks groups of up to 32 bodies, the group criteria up to 64
+    const bool body = c->criterion == HC_CRITERION_BODY;
+    const int gms_body[] = {16, 24, 32}, gms_group[] = {32, 48, 64}, lds[] = {32, 48, 64};
+    for (int gm : body ? gms_body : gms_group)
         for (int ld : lds) cand.push_back(hc_tuning{gm, ld, HC_GROUPS_TREE, 0.0});
     if (c->criterion == HC_CRITERION_BODY)      // the other criteria always walk tree groups
         for (int ld : lds) cand.push_back(hc_tuning{HC_GROUP, ld, HC_GROUPS_CONSECUTIVE, 0.0});

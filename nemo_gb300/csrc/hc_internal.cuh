@@ -19,7 +19,8 @@
 
 #define HC_IMAX (1 << 30)     // defs.h:124-128
 #define HC_MAXLEVEL 31        // levels 0..30
-#define HC_GROUP 32           // bodies per walk group (one warp)
+#define HC_GROUP 32           // bodies per walk group of the per-body rule (one warp, one body per lane)
+#define HC_GROUP2 64          // bodies per walk group of the group criteria (two per lane)
 
 // Device status word (written by kernels, read by the host after a sync).
 // Guard record, kept across evaluations.
@@ -217,6 +218,14 @@ int hc_fma_peak_impl(hc_ctx *c, double *tflops);
             return HC_ERR_CUDA;                                                     \
         }                                                                           \
     } while (0)
+
+// Largest tree-aligned walk group of the build: up to 64 bodies when a
+// group criterion walks the tree, 32 for the per-body rule.
+static inline int hc_table_gmax(const hc_ctx *c)
+{
+    const int cap = c->criterion == 0 ? HC_GROUP : HC_GROUP2;
+    return c->group_max >= 1 && c->group_max <= cap ? c->group_max : cap;
+}
 
 static inline int hc_grid(int64_t n, int block, int cap = 152 * 16)
 {

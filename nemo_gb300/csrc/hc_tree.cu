@@ -473,7 +473,7 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
             nodeA[k] = A;
             nodeB[k] = B;
             nodeQ[2 * (int64_t)k] = make_float4(0.f, 0.f, 0.f, 0.f);
-            nodeQ[2 * (int64_t)k + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            nodeQ[2 * (int64_t)k + 1] = make_float4(0.f, 0.f, 1.f, 0.f);   // no quadrupole, one body, bmax 0
             nodeC[k] = make_int2(-1 - a, D << 8);      // body leaf: -1 - massive rank
             leaf_of_sorted[s] = k;
         } else {
@@ -491,7 +491,7 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
 
 // hackcofm (load.c:183-226), all levels, deepest first, one grid barrier
 // per level.  Children are summed in subindex order exactly as hackcofm does.
-__global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box, const int2 *nodeC, double *nm,
+__global__ void __launch_bounds__(256, 2) k_cofm_all(int usequad, const hc_box *box, const int2 *nodeC, double *nm,
                                                   double *ncx, double *ncy, double *ncz, float4 *nodeA,
                                                   float4 *nodeB, float4 *nodeQ)
 {
@@ -504,14 +504,31 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             const int2 C = nodeC[k];
             if (C.x < 0) continue;                   // body leaf
             const int fc = C.x, nc = C.y & 255;
+            // The children's loads are issued together (predicated on the
+            // child count), not one dependent round trip per child.  FP64 mass
+            // and first moments in hackcofm's order (load.c:193-224; bit-exact).
             double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-            for (int i = 0; i < nc; i++) {
-                const int ch = fc + i;
-                const double mr = nm[ch];
-                m = dadd(m, mr);
-                cx = dadd(cx, dmul(ncx[ch], mr));
-                cy = dadd(cy, dmul(ncy[ch], mr));
-                cz = dadd(cz, dmul(ncz[ch], mr));
+#pragma unroll
+            for (int h = 0; h < 8; h += 4) {
+                double cm[4], px[4], py[4], pz[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    if (h + i < nc) {
+                        cm[i] = nm[fc + h + i];
+                        px[i] = ncx[fc + h + i];
+                        py[i] = ncy[fc + h + i];
+                        pz[i] = ncz[fc + h + i];
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    if (h + i < nc) {
+                        m = dadd(m, cm[i]);
+                        cx = dadd(cx, dmul(px[i], cm[i]));
+                        cy = dadd(cy, dmul(py[i], cm[i]));
+                        cz = dadd(cz, dmul(pz[i], cm[i]));
+                    }
+                }
             }
             cx = ddiv(cx, m);
             cy = ddiv(cy, m);
@@ -523,31 +540,40 @@ __global__ void __launch_bounds__(256) k_cofm_all(int usequad, const hc_box *box
             // children's offsets from the centre of mass in FP32, from the
             // hi + lo positions ((hi - hi) + (lo - lo)): no FP64 work per child.
             // bmax: children's extents shifted to the new centre; Q = sum_child
-            // [ m (3 dr dr^T - |dr|^2 I) + Q_child ], dr = x_child - x_cm
+            // [ m (3 dr dr^T - |dr|^2 I) + Q_child ], dr = x_child - x_cm.
+            // Four children at a time, their loads in flight together.
             float bmax = 0.f, nbody = 0.f;
             float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            for (int i = 0; i < nc; i++) {
-                const int ch = fc + i;
-                const float4 ca = nodeA[ch], cb = nodeB[ch];
-                const float dx = (ca.x - A.x) + (cb.x - B.x), dy = (ca.y - A.y) + (cb.y - B.y),
-                            dz = (ca.z - A.z) + (cb.z - B.z);
-                const bool cell = nodeC[ch].x >= 0;
-                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = make_float4(0.f, 0.f, 1.f, 0.f);
-                if (cell) {
-                    q0 = nodeQ[2 * (int64_t)ch];
-                    q1 = nodeQ[2 * (int64_t)ch + 1];
+#pragma unroll
+            for (int h = 0; h < 8; h += 4) {
+                float4 ca[4], cb[4], q0[4], q1[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int ch = fc + h + i;
+                    if (h + i < nc) {
+                        ca[i] = nodeA[ch];
+                        cb[i] = nodeB[ch];
+                        q1[i] = nodeQ[2 * (int64_t)ch + 1];
+                        if (usequad) q0[i] = nodeQ[2 * (int64_t)ch];
+                    }
                 }
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                bmax = fmaxf(bmax, sqrtf(r2) + q1.w);
-                nbody += q1.z;                   // bodies in the cell (exact below 2^24)
-                if (usequad) {
-                    const float mr = ca.w;
-                    Q[0] += mr * (3.f * dx * dx - r2) + q0.x;
-                    Q[1] += mr * (3.f * dx * dy) + q0.y;
-                    Q[2] += mr * (3.f * dx * dz) + q0.z;
-                    Q[3] += mr * (3.f * dy * dy - r2) + q0.w;
-                    Q[4] += mr * (3.f * dy * dz) + q1.x;
-                    Q[5] += mr * (3.f * dz * dz - r2) + q1.y;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    if (h + i >= nc) continue;
+                    const float dx = (ca[i].x - A.x) + (cb[i].x - B.x), dy = (ca[i].y - A.y) + (cb[i].y - B.y),
+                                dz = (ca[i].z - A.z) + (cb[i].z - B.z);
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    bmax = fmaxf(bmax, sqrtf(r2) + q1[i].w);
+                    nbody += q1[i].z;                // bodies in the cell (exact below 2^24)
+                    if (usequad) {
+                        const float mr = ca[i].w;
+                        Q[0] += mr * (3.f * dx * dx - r2) + q0[i].x;
+                        Q[1] += mr * (3.f * dx * dy) + q0[i].y;
+                        Q[2] += mr * (3.f * dx * dz) + q0[i].z;
+                        Q[3] += mr * (3.f * dy * dy - r2) + q0[i].w;
+                        Q[4] += mr * (3.f * dy * dz) + q1[i].x;
+                        Q[5] += mr * (3.f * dz * dz - r2) + q1[i].y;
+                    }
                 }
             }
             nm[k] = m;
@@ -796,7 +822,7 @@ int hc_tree_build(hc_ctx *c)
     }
 
     // 7. walk groups aligned with the tree
-    const int gmax = c->group_max >= 1 && c->group_max <= HC_GROUP ? c->group_max : HC_GROUP;
+    const int gmax = hc_table_gmax(c);
     k_groups<false><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->pre_b, c->parent, c->nodeC,
                                      c->box, c->maxnode, gmax, c->gcnt, nullptr, nullptr, nullptr);
     hc_scan_exclusive_i32(c, c->gcnt, c->goff, c->maxnode + 1, nullptr);

@@ -55,13 +55,15 @@ struct QueueSmem {
     float z[32];                      // the round's logits
 };
 
+// Interaction lists in pairs: entry e sits in half e & 1 of pair e >> 1, so
+// that both entries' values of one quantity are adjacent floats, the operands
+// of one packed FP32x2 instruction.
 struct WarpSmem {
     uint2 stack[STACK];         // x = first node << 3 | (count - 1), y = lane mask
-    float4 bl[BCAP];            // body list: rel pos (hi), mass
-    float4 bl2[BCAP];           // body list: rel pos (lo), accept mask (bits)
-    float4 cl[CCAP];            // cell list: rel pos, mass
-    float4 cq0[CCAP];           // Qxx Qxy Qxz Qyy
-    float4 cq1[CCAP];           // Qyz Qzz mask(bits) 0
+    float4 bp[BCAP / 2][4];     // body pairs, each quantity for both entries: (hx hy) (hz m) (lx ly) (lz mask)
+                                // (hi and lo parts of the position relative to the group, mass, accept mask)
+    float4 cp[CCAP / 2][5];     // cell pairs, likewise: (x y) (z m) (-Qxx -Qxy) (-Qxz -Qyy) (-Qyz -Qzz)
+    uint2 cmask[CCAP / 2];      // cell pairs: accept masks (per-body rule, counting walk)
     unsigned long long stat[8]; // warp totals (lane 0 writes): see the ST_* indices
     float gu[16];               // the group's uniform values (see GU_* below), read where used
 };
@@ -193,6 +195,12 @@ __device__ __forceinline__ void two_diff(float a, float b, float &s, float &e)
 }
 
 // subdivp in FP64 (grav.c:122-131): open iff tol^2 * |cm - x|^2 < dsq.
+// quantity k (0-based) of list entry e in a pair array with float4 rows
+__device__ __forceinline__ float *pair_slot(float4 *row, int e) { return reinterpret_cast<float *>(row) + (e & 1); }
+__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
+
 __device__ __forceinline__ bool open_exact(double cx, double cy, double cz, double x, double y, double z,
                                            double tol2, double dsq)
 {
@@ -248,9 +256,12 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
 template <bool QUAD, bool COUNT, int MODE>
 // Register budget: 96 (5 blocks of 4 warps per SM) for the per-body rule and
 // the learned walk, 80 (6 blocks) for the group and error rules.
-__global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_walk(WalkArgs g)
+__global__ void __launch_bounds__(WARPS * 32, 5) k_walk(WalkArgs g)
 {
     if (g.run_flag && *g.run_flag == 0) return;   // guard passed: no fallback walk
+    // group criteria accept a cell for the whole group (a cell holding the
+    // group's own bodies is always opened): cell entries need no lane mask
+    constexpr bool MASKED = MODE == 0;
     extern __shared__ float4 smem_raw[];
     WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[threadIdx.x >> 5];
     // MODE 3: per-warp queues after the warp areas; the network's weights are
@@ -258,9 +269,15 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
     QueueSmem *Qs = reinterpret_cast<QueueSmem *>(reinterpret_cast<WarpSmem *>(smem_raw) + WARPS) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
+    // Bodies per lane: the group criteria walk groups of up to 64 bodies
+    // (bodies lane and lane + 32 on each lane: every list entry is loaded
+    // once for both); the per-body rule, whose list entries carry one accept
+    // bit per body, walks groups of up to 32.
+    constexpr int BPL = MODE == 0 ? 1 : 2;
+    constexpr int GW = 32 * BPL;
     const int64_t nmassive = g.use_table ? g.box->nmassive : 0;
     const int64_t ng_table = g.use_table ? g.box->ngroups : 0;
-    const int64_t ngroups = ng_table + (g.ntarget - nmassive + 31) / 32;
+    const int64_t ngroups = ng_table + (g.ntarget - nmassive + GW - 1) / GW;
     const int nnode = g.box->nnode;
     const float tol2 = g.tol2f, eps2 = g.eps2f;
     // warp-uniform totals live in shared memory, not in registers
@@ -281,38 +298,75 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
             s0 = g.gstart[grp];
             cnt = g.gcount[grp];
         } else {
-            s0 = nmassive + (grp - ng_table) * 32;
-            cnt = g.ntarget - s0 < 32 ? g.ntarget - s0 : 32;
+            s0 = nmassive + (grp - ng_table) * GW;
+            cnt = g.ntarget - s0 < GW ? g.ntarget - s0 : GW;
         }
-        const int64_t s = s0 + lane;
-        const bool valid = lane < cnt;
-        const unsigned vmask = __ballot_sync(FULL, valid);
-        const uint32_t o = g.tsorted[valid ? s : s0];
-        const double xd = g.tx[o], yd = g.ty[o], zd = g.tz[o];
+        // the group's bodies; an absent body repeats the lane's first (or the
+        // group's first) so that it changes no group extent
+        bool valid[BPL];
+        uint32_t o[BPL];
+        double xd[BPL], yd[BPL], zd[BPL];
+#pragma unroll
+        for (int k = 0; k < BPL; k++) {
+            valid[k] = lane + 32 * k < cnt;
+            o[k] = valid[k] ? g.tsorted[s0 + lane + 32 * k] : (k == 0 ? g.tsorted[s0] : o[0]);
+            xd[k] = g.tx[o[k]];
+            yd[k] = g.ty[o[k]];
+            zd[k] = g.tz[o[k]];
+        }
+        const unsigned vmask = __ballot_sync(FULL, valid[0]);
 
         // group centre (FP64) and body positions relative to it (FP32)
         double gx, gy, gz;
         {
-            double lox = wmind(xd), hix = wmaxd(xd), loy = wmind(yd), hiy = wmaxd(yd), loz = wmind(zd),
-                   hiz = wmaxd(zd);
-            gx = 0.5 * (lox + hix);
-            gy = 0.5 * (loy + hiy);
-            gz = 0.5 * (loz + hiz);
+            double lox = xd[0], hix = xd[0], loy = yd[0], hiy = yd[0], loz = zd[0], hiz = zd[0];
+#pragma unroll
+            for (int k = 1; k < BPL; k++) {
+                lox = fmin(lox, xd[k]);
+                hix = fmax(hix, xd[k]);
+                loy = fmin(loy, yd[k]);
+                hiy = fmax(hiy, yd[k]);
+                loz = fmin(loz, zd[k]);
+                hiz = fmax(hiz, zd[k]);
+            }
+            gx = 0.5 * (wmind(lox) + wmaxd(hix));
+            gy = 0.5 * (wmind(loy) + wmaxd(hiy));
+            gz = 0.5 * (wmind(loz) + wmaxd(hiz));
         }
         const float ghx = __double2float_rn(gx), ghy = __double2float_rn(gy), ghz = __double2float_rn(gz);
         const float glx = __double2float_rn(gx - (double)ghx), gly = __double2float_rn(gy - (double)ghy),
                     glz = __double2float_rn(gz - (double)ghz);
-        const float bx = __double2float_rn(xd - gx), by = __double2float_rn(yd - gy), bz = __double2float_rn(zd - gz);
         // low parts: body-body separations are formed as (hi - hi) + (lo - lo)
-        const float blx = __double2float_rn((xd - gx) - (double)bx), bly = __double2float_rn((yd - gy) - (double)by),
-                    blz = __double2float_rn((zd - gz) - (double)bz);
-        const float gminx = wmin(bx), gmaxx = wmax(bx), gminy = wmin(by), gmaxy = wmax(by), gminz = wmin(bz),
-                    gmaxz = wmax(bz);
-        const float rg2 = wmax(bx * bx + by * by + bz * bz);
+        float bx[BPL], by[BPL], bz[BPL], blx[BPL], bly[BPL], blz[BPL];
+        float mnx = 3.0e38f, mxx = -3.0e38f, mny = 3.0e38f, mxy = -3.0e38f, mnz = 3.0e38f, mxz = -3.0e38f, r2m = 0.f;
+#pragma unroll
+        for (int k = 0; k < BPL; k++) {
+            bx[k] = __double2float_rn(xd[k] - gx);
+            by[k] = __double2float_rn(yd[k] - gy);
+            bz[k] = __double2float_rn(zd[k] - gz);
+            blx[k] = __double2float_rn((xd[k] - gx) - (double)bx[k]);
+            bly[k] = __double2float_rn((yd[k] - gy) - (double)by[k]);
+            blz[k] = __double2float_rn((zd[k] - gz) - (double)bz[k]);
+            mnx = fminf(mnx, bx[k]);
+            mxx = fmaxf(mxx, bx[k]);
+            mny = fminf(mny, by[k]);
+            mxy = fmaxf(mxy, by[k]);
+            mnz = fminf(mnz, bz[k]);
+            mxz = fmaxf(mxz, bz[k]);
+            r2m = fmaxf(r2m, bx[k] * bx[k] + by[k] * by[k] + bz[k] * bz[k]);
+        }
+        const float gminx = wmin(mnx), gmaxx = wmax(mxx), gminy = wmin(mny), gmaxy = wmax(mxy), gminz = wmin(mnz),
+                    gmaxz = wmax(mxz);
+        const float rg2 = wmax(r2m);
         float amin = 0.f;                        // MODE 2: group's smallest |a| (previous evaluation)
         if (MODE >= 2) {
-            const double axo = g.pax[o], ayo = g.pay[o], azo = g.paz[o];
-            amin = wmin(valid ? __double2float_rn(sqrt(axo * axo + ayo * ayo + azo * azo)) : 3.0e38f);
+            float am = 3.0e38f;
+#pragma unroll
+            for (int k = 0; k < BPL; k++) {
+                const float ax1 = (float)g.pax[o[k]], ay1 = (float)g.pay[o[k]], az1 = (float)g.paz[o[k]];
+                if (valid[k]) am = fminf(am, sqrtf(fmaf(ax1, ax1, fmaf(ay1, ay1, az1 * az1))));
+            }
+            amin = wmin(am);
         }
         const float cR = 2e-6f * tol2 * rg2;     // absolute band term of the FP32 decision
         // Under the group criteria the traversal loop reads these warp-uniform
@@ -329,60 +383,154 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
         }
         __syncwarp();
 
-        float sphi = 0.f, sax = 0.f, say = 0.f, saz = 0.f;   // Kahan sums
-        float cphi = 0.f, cax = 0.f, cay = 0.f, caz = 0.f;
-        int myb = 0, myc = 0;                              // per-body counts
+        float sphi[BPL], sax[BPL], say[BPL], saz[BPL];    // Kahan sums per body
+        float cphi[BPL], cax[BPL], cay[BPL], caz[BPL];
+        int myb[BPL], myc[BPL];                            // per-body counts
+#pragma unroll
+        for (int k = 0; k < BPL; k++) {
+            sphi[k] = sax[k] = say[k] = saz[k] = cphi[k] = cax[k] = cay[k] = caz[k] = 0.f;
+            myb[k] = myc[k] = 0;
+        }
         unsigned gb = 0, gc = 0;                           // this lane's accepted-node interactions
 
+        // The list loops take two entries per step in packed FP32x2
+        // arithmetic (each half rounds as the scalar instruction would); an odd
+        // list is padded with a massless entry far from the group.  Both halves
+        // are summed at the end of the flush, then added with Kahan's rule.
+        // Body entries carry the accept mask (per-body rule) or the group slot
+        // of the body that is the entry itself (group criteria; -1: none).
+        const unsigned lanebit = 1u << lane;
+        auto pad_entry = [&](float4 *row, int e, int nq) {
+            float *f = pair_slot(row, e);
+            f[0] = 1.0e4f;
+            f[2] = 1.0e4f;
+            f[4] = 1.0e4f;
+            for (int k = 3; k < nq; k++) f[2 * k] = 0.f;
+        };
         auto flush_bodies = [&](int nb) {
-            if (lane == 0) S.stat[ST_EB] += nb;
-            float pphi = 0.f, pax = 0.f, pay = 0.f, paz = 0.f;
-            for (int e = 0; e < nb; e++) {
-                const float4 P = S.bl[e];
-                const float4 L = S.bl2[e];
-                const unsigned m = __float_as_uint(L.w);
-                const bool bit = (m >> lane) & 1u;
-                const float dx = (P.x - bx) + (L.x - blx), dy = (P.y - by) + (L.y - bly), dz = (P.z - bz) + (L.z - blz);
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                const float rinv = rsqrtf(r2);
-                const float mr = bit ? P.w * rinv : 0.f;
-                const float mr3 = mr * (rinv * rinv);
-                pphi -= mr;
-                pax = fmaf(mr3, dx, pax);
-                pay = fmaf(mr3, dy, pay);
-                paz = fmaf(mr3, dz, paz);
-                if (COUNT) myb += bit;
+            if (lane == 0) {
+                S.stat[ST_EB] += nb;
+                if (nb & 1) {
+                    pad_entry(S.bp[nb >> 1], nb, 8);
+                    if (MODE != 0) pair_slot(S.bp[nb >> 1], nb)[14] = __int_as_float(-1);
+                }
             }
-            kahan_add(sphi, cphi, pphi);
-            kahan_add(sax, cax, pax);
-            kahan_add(say, cay, pay);
-            kahan_add(saz, caz, paz);
+            __syncwarp();
+            float2 nphi[BPL], ax[BPL], ay[BPL], az[BPL];
+#pragma unroll
+            for (int k = 0; k < BPL; k++) nphi[k] = ax[k] = ay[k] = az[k] = splat2(0.f);
+            const float2 e2 = splat2(eps2);
+            for (int p = 0; p < (nb + 1) >> 1; p++) {
+                const float4 H0 = S.bp[p][0], H1 = S.bp[p][1], L0 = S.bp[p][2], L1 = S.bp[p][3];
+#pragma unroll
+                for (int k = 0; k < BPL; k++) {
+                    const float2 dx = __fadd2_rn(__fadd2_rn(lo2(H0), splat2(-bx[k])), __fadd2_rn(lo2(L0), splat2(-blx[k])));
+                    const float2 dy = __fadd2_rn(__fadd2_rn(hi2(H0), splat2(-by[k])), __fadd2_rn(hi2(L0), splat2(-bly[k])));
+                    const float2 dz = __fadd2_rn(__fadd2_rn(lo2(H1), splat2(-bz[k])), __fadd2_rn(lo2(L1), splat2(-blz[k])));
+                    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+                    bool b0, b1;
+                    if (MODE == 0) {
+                        b0 = __float_as_uint(L1.z) & lanebit;
+                        b1 = __float_as_uint(L1.w) & lanebit;
+                    } else {
+                        b0 = __float_as_int(L1.z) != lane + 32 * k;
+                        b1 = __float_as_int(L1.w) != lane + 32 * k;
+                    }
+                    const float2 w = make_float2(b0 ? rsqrtf(r2.x) : 0.f, b1 ? rsqrtf(r2.y) : 0.f);
+                    const float2 mr = __fmul2_rn(hi2(H1), w);
+                    const float2 mr3 = __fmul2_rn(mr, __fmul2_rn(w, w));
+                    nphi[k] = __fadd2_rn(nphi[k], mr);
+                    ax[k] = __ffma2_rn(mr3, dx, ax[k]);
+                    ay[k] = __ffma2_rn(mr3, dy, ay[k]);
+                    az[k] = __ffma2_rn(mr3, dz, az[k]);
+                    if (COUNT) myb[k] += (int)b0 + (int)b1;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < BPL; k++) {
+                if (COUNT && MODE != 0 && (nb & 1)) myb[k] -= 1;      // the pad counted as a body
+                kahan_add(sphi[k], cphi[k], -(nphi[k].x + nphi[k].y));
+                kahan_add(sax[k], cax[k], ax[k].x + ax[k].y);
+                kahan_add(say[k], cay[k], ay[k].x + ay[k].y);
+                kahan_add(saz[k], caz[k], az[k].x + az[k].y);
+            }
         };
         auto flush_cells = [&](int nc) {
-            if (lane == 0) S.stat[ST_EC] += nc;
-            float pphi = 0.f, pax = 0.f, pay = 0.f, paz = 0.f;
-            // group criteria accept a cell for the whole group (a cell holding
-            // the group's own bodies is always opened): no per-lane mask test
-            constexpr bool MASKED = MODE == 0 || COUNT;
-            for (int e = 0; e < nc; e++) {
-                const float4 P = S.cl[e];
-                const float4 Q1 = (QUAD || MASKED) ? S.cq1[e] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const bool bit = MASKED ? ((__float_as_uint(Q1.z) >> lane) & 1u) : true;
-                const float4 Q0 = QUAD ? S.cq0[e] : make_float4(0.f, 0.f, 0.f, 0.f);
-                cell_term<QUAD>(P, Q0, Q1.x, Q1.y, bit, bx, by, bz, eps2, pphi, pax, pay, paz);
-                if (COUNT) myc += bit;
+            if (lane == 0) {
+                S.stat[ST_EC] += nc;
+                if (nc & 1) {
+                    pad_entry(S.cp[nc >> 1], nc, QUAD ? 10 : 4);
+                    if (MASKED) S.cmask[nc >> 1].y = 0u;
+                }
             }
-            kahan_add(sphi, cphi, pphi);
-            kahan_add(sax, cax, pax);
-            kahan_add(say, cay, pay);
-            kahan_add(saz, caz, paz);
+            __syncwarp();
+            float2 nphi[BPL], ax[BPL], ay[BPL], az[BPL];
+#pragma unroll
+            for (int k = 0; k < BPL; k++) nphi[k] = ax[k] = ay[k] = az[k] = splat2(0.f);
+            const float2 e2 = splat2(eps2);
+            for (int p = 0; p < (nc + 1) >> 1; p++) {
+                const float4 P0 = S.cp[p][0], P1 = S.cp[p][1];
+                bool m0 = true, m1 = true;
+                if (MASKED) {
+                    const uint2 mk = S.cmask[p];
+                    m0 = mk.x & lanebit;
+                    m1 = mk.y & lanebit;
+                    if (COUNT) myc[0] += (int)m0 + (int)m1;
+                }
+                float4 Q0, Q1, Q2;
+                if (QUAD) {
+                    Q0 = S.cp[p][2];
+                    Q1 = S.cp[p][3];
+                    Q2 = S.cp[p][4];
+                }
+#pragma unroll
+                for (int k = 0; k < BPL; k++) {
+                    const float2 dx = __fadd2_rn(lo2(P0), splat2(-bx[k])), dy = __fadd2_rn(hi2(P0), splat2(-by[k])),
+                                 dz = __fadd2_rn(lo2(P1), splat2(-bz[k]));
+                    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+                    float2 w = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                    const float2 rinv2 = __fmul2_rn(w, w);
+                    if (MASKED) w = make_float2(m0 ? w.x : 0.f, m1 ? w.y : 0.f);
+                    const float2 mr = __fmul2_rn(hi2(P1), w);            // m / r (0 for a masked lane)
+                    const float2 mr3 = __fmul2_rn(mr, rinv2);
+                    if (!QUAD) {
+                        nphi[k] = __fadd2_rn(nphi[k], mr);
+                        ax[k] = __ffma2_rn(mr3, dx, ax[k]);
+                        ay[k] = __ffma2_rn(mr3, dy, ay[k]);
+                        az[k] = __ffma2_rn(mr3, dz, az[k]);
+                        continue;
+                    }
+                    // gravsub's quadrupole term (grav.c:62-72) with the list's -Q:
+                    // q = -Q.dr, t = -dr.Q.dr / r^5
+                    const float2 qx = __ffma2_rn(lo2(Q0), dx, __ffma2_rn(hi2(Q0), dy, __fmul2_rn(lo2(Q1), dz)));
+                    const float2 qy = __ffma2_rn(hi2(Q0), dx, __ffma2_rn(hi2(Q1), dy, __fmul2_rn(lo2(Q2), dz)));
+                    const float2 qz = __ffma2_rn(lo2(Q1), dx, __ffma2_rn(lo2(Q2), dy, __fmul2_rn(hi2(Q2), dz)));
+                    const float2 dqd = __ffma2_rn(qx, dx, __ffma2_rn(qy, dy, __fmul2_rn(qz, dz)));
+                    const float2 r5 = __fmul2_rn(__fmul2_rn(w, rinv2), rinv2);
+                    const float2 t = __fmul2_rn(dqd, r5);
+                    // -phi += m/r + dr.Q.dr / (2 r^5);  a += dr (m/r^3 + 5/2 dr.Q.dr/r^7) - Q.dr / r^5
+                    nphi[k] = __ffma2_rn(splat2(-0.5f), t, __fadd2_rn(nphi[k], mr));
+                    const float2 c = __ffma2_rn(__fmul2_rn(splat2(-2.5f), rinv2), t, mr3);
+                    ax[k] = __ffma2_rn(c, dx, __ffma2_rn(r5, qx, ax[k]));
+                    ay[k] = __ffma2_rn(c, dy, __ffma2_rn(r5, qy, ay[k]));
+                    az[k] = __ffma2_rn(c, dz, __ffma2_rn(r5, qz, az[k]));
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < BPL; k++) {
+                if (COUNT && !MASKED) myc[k] += nc;
+                kahan_add(sphi[k], cphi[k], -(nphi[k].x + nphi[k].y));
+                kahan_add(sax[k], cax[k], ax[k].x + ax[k].y);
+                kahan_add(say[k], cay[k], ay[k].x + ay[k].y);
+                kahan_add(saz[k], caz[k], az[k].x + az[k].y);
+            }
         };
 
         int sp = 0, nb = 0, nc = 0;
         bool overflow = false;
         int root = 0;
         if (g.sys_root) {                     // forest: this group's system root
-            root = g.sys_root[g.body_sys[__shfl_sync(FULL, o, 0)]];
+            root = g.sys_root[g.body_sys[__shfl_sync(FULL, o[0], 0)]];
             if (root < 0 || root >= nnode) {
                 if (lane == 0) atomicCAS(&g.st->error, 0, HC_ERR_STATE);
                 continue;
@@ -463,7 +611,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
                 if (have) {
                     const float4 Q0 = g.nodeQ[2 * (int64_t)my_node], Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
                     float f[12];
-                    cell_features_inl(f, q_dmin2, q_dmax2, B.w, A.w, Q1.w, sqrtf(q_dmin2) - Q1.w, Q0, Q1, GUV(13, amin), GUV(12, rg2),
+                    cell_features_inl(f, q_dmin2, q_dmax2, B.w, A.w, Q1.w, q_dmin2 * rsqrtf(q_dmin2) - Q1.w, Q0, Q1, GUV(13, amin), GUV(12, rg2),
                                       eps2, C.y >> 8, (int)cnt,
                                       __log2f(fmaxf(q_err, 1e-38f)) - __log2f(g.eps_acc * GUV(13, amin)));
 #pragma unroll
@@ -479,14 +627,20 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
             const float cx = (A.x - GUV(0, ghx)) + (B.x - GUV(3, glx)), cy = (A.y - GUV(1, ghy)) + (B.y - GUV(4, gly)), cz = (A.z - GUV(2, ghz)) + (B.z - GUV(5, glz));
             const bool isbody = C.x < 0;
             unsigned openm = 0, accm = 0;
+            int selfslot = -1;                 // group criteria: group slot of a body leaf in the group
             bool mixed = false;
             bool band = false;                 // MODE 3: queued for the network
             float bd_dmin2 = 0.f, bd_dmax2 = 0.f, bd_err = 0.f;
             if (have) {
                 if (isbody) {
                     const int64_t slot = (int64_t)(-1 - C.x) - s0;     // leaf holds its massive rank
-                    const unsigned self = (g.self_mode && slot >= 0 && slot < 32) ? (1u << slot) : 0u;
-                    accm = my_mask & ~self;
+                    if (MODE == 0) {
+                        const unsigned self = (g.self_mode && slot >= 0 && slot < 32) ? (1u << slot) : 0u;
+                        accm = my_mask & ~self;
+                    } else {
+                        selfslot = (g.self_mode && slot >= 0 && slot < cnt) ? (int)slot : -1;
+                        accm = cnt > (selfslot >= 0 ? 1 : 0) ? my_mask : 0u;
+                    }
                 } else {
                     const float dsq = B.w;
                     const float ex = fmaxf(0.f, fmaxf(GUV(6, gminx) - cx, cx - GUV(7, gmaxx)));
@@ -508,10 +662,12 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
                     } else if (MODE == 3) {
                         const float4 Q1 = g.nodeQ[2 * (int64_t)my_node + 1];
                         const float b = Q1.w;
-                        const float dmin = sqrtf(dmin2), gap = dmin - b;
+                        // approximate square root and reciprocal: the proxy decides
+                        // nothing exactly (dmin2 = 0 gives a NaN gap: opened)
+                        const float gap = dmin2 * rsqrtf(dmin2) - b;
                         float err = 3.0e38f;           // no expansion (gap <= 0 or size/dmin > 4): open
                         if (gap > 0.f && tmin >= dsq * 0.0625f) {
-                            const float gi = 1.f / gap, bg = b * gi;
+                            const float gi = __fdividef(1.f, gap), bg = b * gi;
                             err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
                         }
                         const float budget = g.eps_acc * GUV(13, amin);
@@ -543,10 +699,10 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
                         }
                     } else if (MODE == 2) {
                         const float b = g.nodeQ[2 * (int64_t)my_node + 1].w;
-                        const float gap = sqrtf(dmin2) - b;
+                        const float gap = dmin2 * rsqrtf(dmin2) - b;          // as in MODE 3
                         bool acc_ok = gap > 0.f && tmin >= dsq * 0.0625f;     // never beyond size/dmin = 4
                         if (acc_ok) {
-                            const float gi = 1.f / gap, bg = b * gi;
+                            const float gi = __fdividef(1.f, gap), bg = b * gi;
                             const float err = A.w * gi * gi * bg * bg * (QUAD ? bg : 1.f);
                             acc_ok = err <= g.eps_acc * GUV(13, amin);
                         }
@@ -587,13 +743,13 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
                 const int jn = __shfl_sync(FULL, my_node, j);
                 const int jdepth = __shfl_sync(FULL, C.y, j) >> 8;
                 const bool in = (jm >> lane) & 1u;
-                const float dx = jx - bx, dy = jy - by, dz = jz - bz;
+                const float dx = jx - bx[0], dy = jy - by[0], dz = jz - bz[0];
                 const float d2 = dx * dx + dy * dy + dz * dz;
                 const float t = tol2 * d2 - jd;
                 bool op = t < 0.f;
                 if (in && fabsf(t) <= 8e-6f * tol2 * d2 + GUV(14, cR)) {
                     // borderline: decide exactly as subdivp does, in FP64
-                    op = open_exact(g.ncx[jn], g.ncy[jn], g.ncz[jn], xd, yd, zd, g.tol2d, g.box->dsq[jdepth]);
+                    op = open_exact(g.ncx[jn], g.ncy[jn], g.ncz[jn], xd[0], yd[0], zd[0], g.tol2d, g.box->dsq[jdepth]);
                     nborder++;
                 }
                 const unsigned ob = __ballot_sync(FULL, in && op), ab = __ballot_sync(FULL, in && !op);
@@ -619,7 +775,8 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
 
             // ---- append accepted nodes to the interaction lists ----
             const bool ab = accm != 0u && isbody, ac = accm != 0u && !isbody;
-            if (COUNT && accm != 0u) atomicAdd(&g.st->mask_hist[__popc(accm)], 1ull);
+            // histogram of the bodies an accepted node serves, in lanes (two bodies per lane for the group criteria)
+            if (COUNT && accm != 0u) atomicAdd(&g.st->mask_hist[MODE == 0 ? __popc(accm) : (int)(cnt + 1) / 2], 1ull);
             const unsigned bbal = __ballot_sync(FULL, ab), cbal = __ballot_sync(FULL, ac);
             if (ab) {
                 // node - centre as an unevaluated float sum hi + lo (TwoSum of the hi parts)
@@ -628,21 +785,35 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
                 two_diff(A.x, GUV(0, ghx), hx, ex);
                 two_diff(A.y, GUV(1, ghy), hy, ey);
                 two_diff(A.z, GUV(2, ghz), hz, ez);
-                S.bl[pos] = make_float4(hx, hy, hz, A.w);
-                S.bl2[pos] = make_float4(ex + (B.x - GUV(3, glx)), ey + (B.y - GUV(4, gly)), ez + (B.z - GUV(5, glz)), __uint_as_float(accm));
-                gb += __popc(accm);
+                float *f = pair_slot(S.bp[pos >> 1], pos);
+                f[0] = hx;
+                f[2] = hy;
+                f[4] = hz;
+                f[6] = A.w;
+                f[8] = ex + (B.x - GUV(3, glx));
+                f[10] = ey + (B.y - GUV(4, gly));
+                f[12] = ez + (B.z - GUV(5, glz));
+                f[14] = MODE == 0 ? __uint_as_float(accm) : __int_as_float(selfslot);
+                gb += MODE == 0 ? __popc(accm) : (unsigned)cnt - (selfslot >= 0 ? 1u : 0u);
             }
             if (ac) {
                 const int pos = nc + __popc(cbal & lt);
-                S.cl[pos] = make_float4(cx, cy, cz, A.w);
+                float *f = pair_slot(S.cp[pos >> 1], pos);
+                f[0] = cx;
+                f[2] = cy;
+                f[4] = cz;
+                f[6] = A.w;
                 if (QUAD) {
                     const float4 q0 = g.nodeQ[2 * (int64_t)my_node], q1 = g.nodeQ[2 * (int64_t)my_node + 1];
-                    S.cq0[pos] = q0;
-                    S.cq1[pos] = make_float4(q1.x, q1.y, __uint_as_float(accm), 0.f);
-                } else {
-                    S.cq1[pos] = make_float4(0.f, 0.f, __uint_as_float(accm), 0.f);
+                    f[8] = -q0.x;
+                    f[10] = -q0.y;
+                    f[12] = -q0.z;
+                    f[14] = -q0.w;
+                    f[16] = -q1.x;
+                    f[18] = -q1.y;
                 }
-                gc += __popc(accm);
+                if (MASKED) (pos & 1 ? S.cmask[pos >> 1].y : S.cmask[pos >> 1].x) = accm;
+                gc += MODE == 0 ? __popc(accm) : (unsigned)cnt;
             }
             nb += __popc(bbal);
             nc += __popc(cbal);
@@ -681,23 +852,26 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 || MODE == 3 ? 5 : 6) k_
         }
         __syncwarp();
 
-        if (valid) {
-            const double rphi = (double)sphi - (double)cphi;
-            const double rax = (double)sax - (double)cax, ray = (double)say - (double)cay,
-                         raz = (double)saz - (double)caz;
+#pragma unroll
+        for (int k = 0; k < BPL; k++) {
+            if (!valid[k]) continue;
+            const uint32_t ok = o[k];
+            const double rphi = (double)sphi[k] - (double)cphi[k];
+            const double rax = (double)sax[k] - (double)cax[k], ray = (double)say[k] - (double)cay[k],
+                         raz = (double)saz[k] - (double)caz[k];
             if (g.kick_dthf != 0.0 && g.nstep > 0) {
                 // closing half kick with the new acceleration (code.c:175-179)
-                g.vx[o] = __dadd_rn(g.vx[o], __dmul_rn(__dsub_rn(rax, g.oax[o]), g.kick_dthf));
-                g.vy[o] = __dadd_rn(g.vy[o], __dmul_rn(__dsub_rn(ray, g.oay[o]), g.kick_dthf));
-                g.vz[o] = __dadd_rn(g.vz[o], __dmul_rn(__dsub_rn(raz, g.oaz[o]), g.kick_dthf));
+                g.vx[ok] = __dadd_rn(g.vx[ok], __dmul_rn(__dsub_rn(rax, g.oax[ok]), g.kick_dthf));
+                g.vy[ok] = __dadd_rn(g.vy[ok], __dmul_rn(__dsub_rn(ray, g.oay[ok]), g.kick_dthf));
+                g.vz[ok] = __dadd_rn(g.vz[ok], __dmul_rn(__dsub_rn(raz, g.oaz[ok]), g.kick_dthf));
             }
-            g.oax[o] = rax;
-            g.oay[o] = ray;
-            g.oaz[o] = raz;
-            g.ophi[o] = rphi;
+            g.oax[ok] = rax;
+            g.oay[ok] = ray;
+            g.oaz[ok] = raz;
+            g.ophi[ok] = rphi;
             if (COUNT) {
-                g.cnt_b[o] = myb;
-                g.cnt_c[o] = myc;
+                g.cnt_b[ok] = myb[k];
+                g.cnt_c[ok] = myc[k];
             }
         }
     }
@@ -801,7 +975,11 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
     a.paz = c->az;
     a.gstart = c->gstart;
     a.gcount = c->gcount;
-    a.use_table = (self && (c->group_kind == 1 || c->criterion != HC_CRITERION_BODY)) ? 1 : 0;
+    // group criteria walk the tree groups (up to 64 bodies); the per-body
+    // rule walks them when chosen and they hold at most 32 bodies (its own
+    // criterion), else 32 consecutive bodies (also the guard's fallback walk)
+    const bool per_body = body_rule || c->criterion == HC_CRITERION_BODY;
+    a.use_table = (self && (!per_body || (c->criterion == HC_CRITERION_BODY && c->group_kind == 1))) ? 1 : 0;
     HC_CUDA(cudaMemsetAsync(a.group_counter, 0, sizeof(unsigned), c->stream));
     const bool count = c->prm.count_per_body && self && c->cnt_b;
     const int v = (c->prm.usequad ? 2 : 0) + (count ? 1 : 0);
@@ -902,19 +1080,38 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
     if (i >= nsample) return;
     const int grp = sample_group[i], node = sample_node[i];
     const int s0 = gstart[grp], cnt = gcount[grp];
-    const bool valid = lane < cnt;
-    const uint32_t o = tord[valid ? s0 + lane : s0];
-    const double xd = px[o], yd = py[o], zd = pz[o];
-    const double gx = 0.5 * (wmind(xd) + wmaxd(xd)), gy = 0.5 * (wmind(yd) + wmaxd(yd)),
-                 gz = 0.5 * (wmind(zd) + wmaxd(zd));
+    // groups of up to 64 bodies: bodies lane and lane + 32 on each lane
+    constexpr int BPL = 2;
+    bool valid[BPL];
+    uint32_t o[BPL];
+    double xd[BPL], yd[BPL], zd[BPL];
+#pragma unroll
+    for (int k = 0; k < BPL; k++) {
+        valid[k] = lane + 32 * k < cnt;
+        o[k] = valid[k] ? tord[s0 + lane + 32 * k] : (k == 0 ? tord[s0] : o[0]);
+        xd[k] = px[o[k]];
+        yd[k] = py[o[k]];
+        zd[k] = pz[o[k]];
+    }
+    const double gx = 0.5 * (wmind(fmin(xd[0], xd[1])) + wmaxd(fmax(xd[0], xd[1]))),
+                 gy = 0.5 * (wmind(fmin(yd[0], yd[1])) + wmaxd(fmax(yd[0], yd[1]))),
+                 gz = 0.5 * (wmind(fmin(zd[0], zd[1])) + wmaxd(fmax(zd[0], zd[1])));
     const float ghx = __double2float_rn(gx), ghy = __double2float_rn(gy), ghz = __double2float_rn(gz);
     const float glx = __double2float_rn(gx - (double)ghx), gly = __double2float_rn(gy - (double)ghy),
                 glz = __double2float_rn(gz - (double)ghz);
-    const float bx = __double2float_rn(xd - gx), by = __double2float_rn(yd - gy), bz = __double2float_rn(zd - gz);
-    const float gminx = wmin(bx), gmaxx = wmax(bx), gminy = wmin(by), gmaxy = wmax(by), gminz = wmin(bz),
-                gmaxz = wmax(bz);
+    float bx[BPL], by[BPL], bz[BPL], amag[BPL];
+#pragma unroll
+    for (int k = 0; k < BPL; k++) {
+        bx[k] = __double2float_rn(xd[k] - gx);
+        by[k] = __double2float_rn(yd[k] - gy);
+        bz[k] = __double2float_rn(zd[k] - gz);
+        const uint32_t q = o[k];
+        amag[k] = (float)sqrt(ax[q] * ax[q] + ay[q] * ay[q] + az[q] * az[q]);
+    }
+    const float gminx = wmin(fminf(bx[0], bx[1])), gmaxx = wmax(fmaxf(bx[0], bx[1])),
+                gminy = wmin(fminf(by[0], by[1])), gmaxy = wmax(fmaxf(by[0], by[1])),
+                gminz = wmin(fminf(bz[0], bz[1])), gmaxz = wmax(fmaxf(bz[0], bz[1]));
     const float eps2 = g.eps2f;
-    const float amag = (float)sqrt(ax[o] * ax[o] + ay[o] * ay[o] + az[o] * az[o]);
     auto rel_pos = [&](int k, float &cx, float &cy, float &cz) {
         const float4 A = g.nodeA[k], B = g.nodeB[k];
         cx = (A.x - ghx) + (B.x - glx);
@@ -923,15 +1120,22 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
         return A.w;
     };
     // multipole of the sampled cell
-    float mphi = 0.f, max_ = 0.f, may = 0.f, maz = 0.f;
+    float mphi[BPL], max_[BPL], may[BPL], maz[BPL];
     {
         float cx, cy, cz;
         const float m = rel_pos(node, cx, cy, cz);
         const float4 Q0 = g.nodeQ[2 * (int64_t)node], Q1 = g.nodeQ[2 * (int64_t)node + 1];
-        cell_term<QUAD>(make_float4(cx, cy, cz, m), Q0, Q1.x, Q1.y, valid, bx, by, bz, eps2, mphi, max_, may, maz);
+#pragma unroll
+        for (int k = 0; k < BPL; k++) {
+            mphi[k] = max_[k] = may[k] = maz[k] = 0.f;
+            cell_term<QUAD>(make_float4(cx, cy, cz, m), Q0, Q1.x, Q1.y, valid[k], bx[k], by[k], bz[k], eps2, mphi[k],
+                            max_[k], may[k], maz[k]);
+        }
     }
     // refined reference over the subtree
-    float rphi = 0.f, rax = 0.f, ray = 0.f, raz = 0.f;
+    float rphi[BPL], rax[BPL], ray[BPL], raz[BPL];
+#pragma unroll
+    for (int k = 0; k < BPL; k++) rphi[k] = rax[k] = ray[k] = raz[k] = 0.f;
     int sp = 0;
     {
         const int2 C = g.nodeC[node];
@@ -950,8 +1154,10 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
         float cx, cy, cz;
         const float m = rel_pos(k, cx, cy, cz);
         if (C.x < 0) {
-            cell_term<false>(make_float4(cx, cy, cz, m), make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, valid, bx, by, bz,
-                             eps2, rphi, rax, ray, raz);
+#pragma unroll
+            for (int j = 0; j < BPL; j++)
+                cell_term<false>(make_float4(cx, cy, cz, m), make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, valid[j], bx[j],
+                                 by[j], bz[j], eps2, rphi[j], rax[j], ray[j], raz[j]);
             continue;
         }
         const float ex = fmaxf(0.f, fmaxf(gminx - cx, cx - gmaxx)), ey = fmaxf(0.f, fmaxf(gminy - cy, cy - gmaxy)),
@@ -960,8 +1166,11 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
         const float4 Q1 = g.nodeQ[2 * (int64_t)k + 1];
         const float b = Q1.w;
         if (dmin - b > 10.f * b) {
-            cell_term<QUAD>(make_float4(cx, cy, cz, m), g.nodeQ[2 * (int64_t)k], Q1.x, Q1.y, valid, bx, by, bz, eps2,
-                            rphi, rax, ray, raz);
+            const float4 Q0 = g.nodeQ[2 * (int64_t)k];
+#pragma unroll
+            for (int j = 0; j < BPL; j++)
+                cell_term<QUAD>(make_float4(cx, cy, cz, m), Q0, Q1.x, Q1.y, valid[j], bx[j], by[j], bz[j], eps2,
+                                rphi[j], rax[j], ray[j], raz[j]);
         } else {
             const int nc = C.y & 255;
             if (sp + nc > LSTACK) break;          // cannot happen for depth <= 31; stop rather than overflow
@@ -970,8 +1179,12 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
             __syncwarp();
         }
     }
-    const float dx = max_ - rax, dy = may - ray, dz = maz - raz;
-    const float rel = valid && amag > 0.f ? sqrtf(dx * dx + dy * dy + dz * dz) / amag : 0.f;
+    float rel = 0.f;
+#pragma unroll
+    for (int k = 0; k < BPL; k++) {
+        const float dx = max_[k] - rax[k], dy = may[k] - ray[k], dz = maz[k] - raz[k];
+        if (valid[k] && amag[k] > 0.f) rel = fmaxf(rel, sqrtf(dx * dx + dy * dy + dz * dz) / amag[k]);
+    }
     const float rmax = wmax(rel);
     if (lane == 0) {
         y[i] = rmax <= eps_label ? 1.f : 0.f;

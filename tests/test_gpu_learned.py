@@ -174,10 +174,11 @@ def test_guard(hc, plummer):
         ctx.set_guard(N_PLUMMER + 1, 1e-3)
     with pytest.raises(hc.HCError):
         ctx.set_guard(256, 0.0)
-    # per-body rule: reference forces and counts.  The fallback walks tree
-    # groups (as the approximate criteria do); the per-body rule's interaction
-    # sets do not depend on the grouping, the rounding of its FP32 sums does.
-    ctx.set_grouping("tree")
+    # per-body rule: reference forces and counts.  The fallback walks 32
+    # consecutive bodies per group (the approximate criteria's tree groups hold
+    # up to 64); the per-body rule's interaction sets do not depend on the
+    # grouping, the rounding of its FP32 sums does.
+    ctx.set_grouping("consecutive")
     ctx.evaluate()
     db = ctx.diagnostics()
     _, acc_body, phi_body = ctx.download(phase=False)
@@ -217,7 +218,7 @@ def test_guard(hc, plummer):
 
     # leapfrog steps with a failing guard follow the per-body rule's run
     ref = hc.Context(N_PLUMMER, tol=0.5, eps=0.01, usequad=True)
-    ref.set_grouping("tree")
+    ref.set_grouping("consecutive")
     for c in (ctx, ref):
         c.upload(m, ph)
     ctx.set_criterion("body")
