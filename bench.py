@@ -344,10 +344,13 @@ def run_ours(args, world, rank, local):
     t0 = time.perf_counter()
     set_mode(ctx, ("body", TOL))
     ctx.evaluate()
-    train = ctx.learn_from_self(theta=0.03, target=1 << 20)
+    tg = TUNING["group"]                     # labels from the groups the learned walk uses
+    ctx.set_tuning(tg["group_max"], tg["list_depth"], tg["grouping"])
+    train = ctx.learn_from_self(theta=args.train_theta, target=1 << 20, band=tuple(args.train_band))
     torch.cuda.synchronize()
     train["seconds"] = time.perf_counter() - t0
-    ctx.learn_band(0.5, 3.0)
+    train["band"] = list(args.band)
+    ctx.learn_band(*args.band)
 
     # ---- calibration to equal RMS (untimed) ----
     fixed = point(ctx, ("body", TOL), idx, ea)
@@ -598,8 +601,10 @@ def run_galaxy(args, world, rank, local):
     rng = np.random.default_rng(12345)
     idx = np.sort(rng.choice(n, size=min(args.sample, 4096), replace=False)).astype(np.int64)
     ea, _ = ctx.direct_sample(idx)
-    train = ctx.learn_from_self(theta=0.03, target=1 << 20)
-    ctx.learn_band(0.5, 3.0)
+    tg = TUNING["group"]                     # labels from the groups the learned walk uses
+    ctx.set_tuning(tg["group_max"], tg["list_depth"], tg["grouping"])
+    train = ctx.learn_from_self(theta=args.train_theta, target=1 << 20, band=tuple(args.train_band))
+    ctx.learn_band(*args.band)
     fixed = point(ctx, ("body", TOL), idx, ea)
     lrn_pt, cal = calibrate(ctx, idx, ea, lambda e: ("learned", e, LEARNED_THRESHOLD), 1e-3, 64.0, fixed["rms"],
                             steps=5)
@@ -693,6 +698,11 @@ def main():
                     help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
                          "ensemble: 4096 independent systems; galaxy: 2^24-body disk galaxy, leapfrog")
     ap.add_argument("--nsys", type=int, default=ENS_NSYS)
+    ap.add_argument("--train-theta", type=float, default=0.03, help="learned criterion: error budget of the label walk")
+    ap.add_argument("--train-band", type=float, nargs=2, default=[1.0, 16.0],
+                    help="learned criterion: proxy band (x budget) sampled for training")
+    ap.add_argument("--band", type=float, nargs=2, default=[0.5, 16.0],
+                    help="learned criterion: proxy band (x budget) the network decides in the walk")
     ap.add_argument("--generator", default="host", choices=["host", "device"],
                     help="galaxy workload: draw the bodies with mkgalaxy on the host or hc_generate on the device")
     args = ap.parse_args()

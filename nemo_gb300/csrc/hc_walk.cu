@@ -256,7 +256,7 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
 template <bool QUAD, bool COUNT, int MODE>
 // Register budget: 96 (5 blocks of 4 warps per SM) for the per-body rule and
 // the learned walk, 80 (6 blocks) for the group and error rules.
-__global__ void __launch_bounds__(WARPS * 32, 5) k_walk(WalkArgs g)
+__global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs g)
 {
     if (g.run_flag && *g.run_flag == 0) return;   // guard passed: no fallback walk
     // group criteria accept a cell for the whole group (a cell holding the
@@ -264,9 +264,14 @@ __global__ void __launch_bounds__(WARPS * 32, 5) k_walk(WalkArgs g)
     constexpr bool MASKED = MODE == 0;
     extern __shared__ float4 smem_raw[];
     WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[threadIdx.x >> 5];
-    // MODE 3: per-warp queues after the warp areas; the network's weights are
-    // read through L1 from global memory (small, shared by every warp)
+    // MODE 3: per-warp queues after the warp areas, then the network's
+    // weights, copied once per block (14 KB, read by every warp's rounds)
     QueueSmem *Qs = reinterpret_cast<QueueSmem *>(reinterpret_cast<WarpSmem *>(smem_raw) + WARPS) + (threadIdx.x >> 5);
+    MlpSmem *Ms = reinterpret_cast<MlpSmem *>(reinterpret_cast<QueueSmem *>(reinterpret_cast<WarpSmem *>(smem_raw) + WARPS) + WARPS);
+    if (MODE == 3 && g.mlp) {
+        mlp_load(*Ms, g.mlp);
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     // Bodies per lane: the group criteria walk groups of up to 64 bodies
@@ -622,7 +627,7 @@ __global__ void __launch_bounds__(WARPS * 32, 5) k_walk(WalkArgs g)
 #pragma unroll
                 for (int k = 6; k < MLP_XS / 2; k++) row[k] = 0u;
                 __syncwarp();
-                logit = mlp_warp_lean(*g.mlp, Qs->x, Qs->z, ncand);
+                logit = mlp_warp_lean(*Ms, Qs->x, Qs->z, ncand);
             }
             const float cx = (A.x - GUV(0, ghx)) + (B.x - GUV(3, glx)), cy = (A.y - GUV(1, ghy)) + (B.y - GUV(4, gly)), cz = (A.z - GUV(2, ghz)) + (B.z - GUV(5, glz));
             const bool isbody = C.x < 0;
@@ -895,7 +900,10 @@ __global__ void __launch_bounds__(WARPS * 32, 5) k_walk(WalkArgs g)
     }
 }
 
-constexpr size_t walk_smem(int mode) { return sizeof(WarpSmem) * WARPS + (mode == 3 ? sizeof(QueueSmem) * WARPS : 0); }
+constexpr size_t walk_smem(int mode)
+{
+    return sizeof(WarpSmem) * WARPS + (mode == 3 ? sizeof(QueueSmem) * WARPS + sizeof(MlpSmem) : 0);
+}
 
 template <bool Q, bool C, int M>
 int configure(hc_ctx *c, int variant)
