@@ -439,7 +439,9 @@ def run_ours(args, world, rank, local):
                 traffic = t.get("learned" if head_mode[0] == "learned" else "body")
         except (OSError, ValueError):
             traffic = None
-    ws["mask_fill"] = (head["n2b"] + head["nbc"]) / max(1, 32 * (ws["entries_body"] + ws["entries_cell"]))
+    # body slots per list entry: 32 lanes, two bodies each under the group criteria
+    slots = 32 if head_mode[0] == "body" else 64
+    ws["mask_fill"] = (head["n2b"] + head["nbc"]) / max(1, slots * (ws["entries_body"] + ws["entries_cell"]))
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
