@@ -132,7 +132,7 @@ int alloc_all(hc_ctx *c)
     HC_TRY(dalloc(c, &c->flags, 4 * n + 8));
     HC_TRY(dalloc(c, &c->scan_tmp, 1024));
     const int64_t big = std::max<int64_t>(n, mn);
-    HC_TRY(dalloc(c, &c->hist, 256 * ((big + 4095) / 4096) + 256));
+    HC_TRY(dalloc(c, &c->hist, hc_sort_scratch_words(big)));
     HC_TRY(dalloc(c, &c->cand, n));
     HC_TRY(dalloc(c, &c->ncand, 4));
     HC_TRY(dalloc(c, &c->diag_part, 36 * 1024));
@@ -175,7 +175,7 @@ int ensure_test_capacity(hc_ctx *c, int64_t nt)
     // the radix sort histograms are sized for max(n, maxnode); grow if needed
     if (nt > std::max<int64_t>(c->n, c->maxnode)) {
         cudaFree(c->hist);
-        HC_TRY(dalloc(c, &c->hist, 256 * ((nt + 4095) / 4096) + 256));
+        HC_TRY(dalloc(c, &c->hist, hc_sort_scratch_words(nt)));
     }
     c->tcap = nt;
     return HC_OK;

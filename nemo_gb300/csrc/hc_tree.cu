@@ -376,12 +376,12 @@ __global__ void k_cell_end(const unsigned long long *mhi, const uint32_t *mlo, c
     }
 }
 
-__global__ void k_levels(const uint32_t *offs, int nblk, hc_box *box)
+__global__ void k_levels(const uint32_t *offs, hc_box *box)
 {
-    // offs is the scanned depth histogram (digit-major); digit D starts at offs[D*nblk]
+    // offs: the depth sort's digit offsets (exclusive scan of its depth counts)
     int D = threadIdx.x;
     if (D <= HC_MAXLEVEL + 1) {
-        int v = D <= HC_MAXLEVEL ? (int)offs[(int64_t)D * nblk] : box->nnode;
+        int v = D <= HC_MAXLEVEL ? (int)offs[D] : box->nnode;
         if (v > box->nnode) v = box->nnode;
         box->level_start[D] = v;
     }
@@ -793,7 +793,7 @@ int hc_tree_build(hc_ctx *c)
     uint32_t *nolo[2] = {nullptr, nullptr};
     int dsel = hc_radix_sort_keys(c, c->dkey, nolo, c->dval, c->maxnode, 0, 8, false, &c->box->nnode);
     c->bfs2pre = c->dval[dsel];
-    k_levels<<<1, 64, 0, s>>>(c->hist, (int)((c->maxnode + 4095) / 4096), c->box);
+    k_levels<<<1, 64, 0, s>>>(c->hist, c->box);      // the sort leaves its digit offsets at hist[0..255]
     k_pre2bfs<<<Gn, B, 0, s>>>(c->bfs2pre, c->box, c->pre2bfs);
     k_parent<<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_info, c->box, c->parent);
     k_clear_links<<<Gn, B, 0, s>>>(c->box, c->maxnode, c->nodeC, c->lastc);
@@ -835,6 +835,7 @@ int hc_tree_build(hc_ctx *c)
 
 int hc_tree_setup(hc_ctx *c)
 {
+    if (int r = hc_sort_setup(c)) return r;
     int dev = 0, nsm = 0, per = 0;
     HC_CUDA(cudaGetDevice(&dev));
     HC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
