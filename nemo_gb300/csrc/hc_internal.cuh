@@ -110,6 +110,8 @@ struct hc_ctx {
     uint32_t *dval[2];
     uint32_t *bfs2pre, *pre2bfs;
     int32_t *parent, *lastc;
+    int32_t *cperm;           // upward pass: cells grouped by depth, then child count
+    uint32_t *cbins;          // their group offsets [257] and placement cursors [256]
     float4 *nodeA, *nodeB, *nodeQ;
     int2 *nodeC;
     double *nm, *ncx, *ncy, *ncz;         // FP64 mass and centre of mass per node

@@ -70,19 +70,32 @@ __global__ void k_scan_parts(T *part, int nparts, T *total)
     if (threadIdx.x == 0 && total) *total = tot;
 }
 
-// Phase 3: scan each chunk in tiles of blockDim, offset by its block prefix.
+// Phase 3: scan each chunk, offset by its block prefix, in steps of
+// blockDim x SCAN_ITEMS elements (each thread scans its consecutive items
+// serially; one block scan per step).  In place is allowed: a thread reads
+// its items before writing them.
+constexpr int SCAN_ITEMS = 8;
 template <typename T>
 __global__ void k_scan_down(const T *in, T *out, int64_t n, int64_t chunk, const T *part)
 {
     __shared__ T sh[32];
     int64_t beg = (int64_t)blockIdx.x * chunk, end = min(beg + chunk, n);
     T carry = part[blockIdx.x];
-    for (int64_t t = beg; t < end; t += blockDim.x) {
-        int64_t i = t + threadIdx.x;
-        T v = i < end ? in[i] : T(0);
+    for (int64_t t = beg; t < end; t += (int64_t)blockDim.x * SCAN_ITEMS) {
+        const int64_t i0 = t + (int64_t)threadIdx.x * SCAN_ITEMS;
+        T v[SCAN_ITEMS], s = T(0);
+#pragma unroll
+        for (int j = 0; j < SCAN_ITEMS; j++) {
+            v[j] = i0 + j < end ? in[i0 + j] : T(0);
+            s += v[j];
+        }
         T tot;
-        T ex = block_exclusive_scan<T>(v, sh, &tot);
-        if (i < end) out[i] = carry + ex;
+        T run = carry + block_exclusive_scan<T>(s, sh, &tot);
+#pragma unroll
+        for (int j = 0; j < SCAN_ITEMS; j++) {
+            if (i0 + j < end) out[i0 + j] = run;
+            run += v[j];
+        }
         carry += tot;
     }
 }

@@ -491,18 +491,89 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
 
 // hackcofm (load.c:183-226), all levels, deepest first, one grid barrier
 // per level.  Children are summed in subindex order exactly as hackcofm does.
+// The upward pass takes each level's cells only, grouped by child count: the
+// cells of a warp then run the same number of FP64 child steps and no lane
+// idles on a body leaf (the levels interleave cells and leaves in key order).
+// Group of a cell: depth * 8 + (children - 1); order inside a group is free.
+__device__ __forceinline__ int cell_group(int2 C) { return min((C.y >> 8), 31) * 8 + (C.y & 255) - 1; }
+
+__global__ void k_cell_count(const int2 *nodeC, const hc_box *box, uint32_t *cnt)
+{
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int nn = box->nnode;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+        const int2 C = nodeC[k];
+        if (C.x >= 0 && (C.y & 255) >= 1) atomicAdd(&h[cell_group(C)], 1u);
+    }
+    __syncthreads();
+    if (h[threadIdx.x]) atomicAdd(&cnt[threadIdx.x], h[threadIdx.x]);
+}
+
+// group offsets off[0..256] (exclusive scan of the 256 counts) and placement
+// cursors cur[0..255]; one block of 256 threads: warp scans, then the warp sums
+__global__ void k_cell_offsets(uint32_t *off, uint32_t *cur)
+{
+    __shared__ uint32_t wsum[8];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint32_t v = off[t];
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int i = 0; i < w; i++) before += wsum[i];
+    const uint32_t ex = before + x - v;
+    off[t] = ex;
+    cur[t] = ex;
+    if (t == 255) off[256] = ex + v;
+}
+
+// places each block's cells: one reservation per group per block, then slots
+// handed out inside the reservation
+__global__ void k_cell_place(const int2 *nodeC, const hc_box *box, uint32_t *cur, int32_t *perm)
+{
+    __shared__ uint32_t h[256], base[256];
+    const int nn = box->nnode;
+    for (int k0 = blockIdx.x * blockDim.x; k0 < nn; k0 += gridDim.x * blockDim.x) {
+        const int k = k0 + threadIdx.x;
+        h[threadIdx.x] = 0;
+        __syncthreads();
+        int grp = -1, slot = 0;
+        if (k < nn) {
+            const int2 C = nodeC[k];
+            if (C.x >= 0 && (C.y & 255) >= 1) {
+                grp = cell_group(C);
+                slot = (int)atomicAdd(&h[grp], 1u);
+            }
+        }
+        __syncthreads();
+        if (h[threadIdx.x]) base[threadIdx.x] = atomicAdd(&cur[threadIdx.x], h[threadIdx.x]);
+        __syncthreads();
+        if (grp >= 0) perm[base[grp] + slot] = k;
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(256, 2) k_cofm_all(int usequad, const hc_box *box, const int2 *nodeC, double *nm,
-                                                  double *ncx, double *ncy, double *ncz, float4 *nodeA,
-                                                  float4 *nodeB, float4 *nodeQ)
+                                                     double *ncx, double *ncy, double *ncz, float4 *nodeA,
+                                                     float4 *nodeB, float4 *nodeQ, const int32_t *cperm,
+                                                     const uint32_t *coff)
 {
     cg::grid_group grid = cg::this_grid();
     const int maxd = box->nnode > 0 ? box->max_depth : -1;
     for (int D = maxd; D >= 0; D--) {
-        const int ls = box->level_start[D], le = box->level_start[D + 1];
+        // the level's cells only, grouped by child count (coff: group offsets)
+        const int ls = (int)coff[D * 8], le = (int)coff[D * 8 + 8];
         const float dsqf = __double2float_rn(box->dsq[D]);
-        for (int k = ls + (int)grid.thread_rank(); k < le; k += (int)grid.size()) {
+        for (int j = ls + (int)grid.thread_rank(); j < le; j += (int)grid.size()) {
+            const int k = cperm[j];
             const int2 C = nodeC[k];
-            if (C.x < 0) continue;                   // body leaf
             const int fc = C.x, nc = C.y & 255;
             // The children's loads are issued together (predicated on the
             // child count), not one dependent round trip per child.  FP64 mass
@@ -803,11 +874,17 @@ int hc_tree_build(hc_ctx *c)
                                  c->ncy, c->ncz, c->leaf_of_sorted, c->st);
     c->launches += 7;
 
-    // 6. upward pass, deepest level first, one cooperative launch
+    // 6. upward pass, deepest level first, one cooperative launch, over the
+    // cells grouped by depth and child count
+    HC_CUDA(cudaMemsetAsync(c->cbins, 0, sizeof(uint32_t) * 520, s));
+    k_cell_count<<<Gn, B, 0, s>>>(c->nodeC, c->box, c->cbins);
+    k_cell_offsets<<<1, 256, 0, s>>>(c->cbins, c->cbins + 260);
+    k_cell_place<<<Gn, B, 0, s>>>(c->nodeC, c->box, c->cbins + 260, c->cperm);
+    c->launches += 3;
     {
         int usequad = c->prm.usequad;
         void *args[] = {&usequad, &c->box, &c->nodeC, &c->nm, &c->ncx, &c->ncy, &c->ncz, &c->nodeA, &c->nodeB,
-                        &c->nodeQ};
+                        &c->nodeQ, &c->cperm, &c->cbins};
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(c->cofm_grid);
         cfg.blockDim = dim3(256);
