@@ -151,16 +151,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_hist(const unsigned long 
     __shared__ uint32_t h[NPASS_MAX][256];
     for (int p = 0; p < NPASS_MAX; p++) h[p][threadIdx.x] = 0;
     __syncthreads();
-    const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
-    for (int64_t t = (int64_t)blockIdx.x * SORT_THREADS; t < n; t += (int64_t)gridDim.x * SORT_THREADS) {
-        const int64_t i = t + threadIdx.x;
-        const bool valid = i < n;
-        const unsigned long long k = valid ? khi[i] : 0ull;
-        for (int p = 0; p < npass; p++) {
-            const int d = valid ? (int)((k >> (begin_bit + 8 * p)) & 255u) : 256 + (int)(threadIdx.x & 31);
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            if (valid && (peers & lt) == 0) atomicAdd(&h[p][d], (uint32_t)__popc(peers));
-        }
+    for (int64_t i = (int64_t)blockIdx.x * SORT_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * SORT_THREADS) {
+        const unsigned long long k = khi[i];
+        for (int p = 0; p < npass; p++) atomicAdd(&h[p][(k >> (begin_bit + 8 * p)) & 255u], 1u);
     }
     __syncthreads();
     for (int p = 0; p < npass; p++)

@@ -69,15 +69,44 @@ __device__ __forceinline__ bool inbox(double x, double y, double z, const double
 
 // ---------------- expandbox replay ----------------
 
+// FP32 value of a double from its high word (sign, exponent, top 20 mantissa
+// bits) with integer operations only: relative error below 2^-20; false for
+// zeros, denormals, infinities, NaNs and magnitudes outside the FP32 range.
+__device__ __forceinline__ bool approx_f32(double x, float *f)
+{
+    const int hi = __double2hiint(x);
+    const int e = ((hi >> 20) & 0x7ff) - 1023 + 127;
+    if (e < 1 || e > 254) return false;
+    *f = __int_as_float((hi & (int)0x80000000) | (e << 23) | ((hi & 0xfffff) << 3));
+    return true;
+}
+
+// Massive flags, and whether a massive body lies outside the box (intcoord's
+// test, load.c:135-156).  A body clearly inside by an FP32 estimate with a
+// margin far above its error skips the exact FP64 test (the FP64 pipe runs at
+// about 1/60 of the FP32 rate); the rest take it.
 __global__ void k_box_flags(const double *mass, const double *px, const double *py, const double *pz,
                             int64_t n, const hc_box *box, int32_t *outside, int32_t *massive)
 {
     double rmin[3] = {box->rmin[0], box->rmin[1], box->rmin[2]};
     double rsize = box->rsize;
+    const float lo[3] = {(float)rmin[0], (float)rmin[1], (float)rmin[2]}, sz = (float)rsize;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         bool m = mass[i] != 0.0;
         massive[i] = m;
-        outside[i] = m && !inbox(px[i], py[i], pz[i], rmin, rsize);
+        const double x[3] = {px[i], py[i], pz[i]};
+        bool clear = true;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            float f;
+            if (!approx_f32(x[k], &f)) {
+                clear = false;
+                continue;
+            }
+            const float u = f - lo[k], margin = 0x1p-16f * sz + 0x1p-18f * fabsf(f);
+            clear = clear && u >= margin && u <= sz - margin;
+        }
+        outside[i] = m && !(clear || inbox(x[0], x[1], x[2], rmin, rsize));
     }
 }
 

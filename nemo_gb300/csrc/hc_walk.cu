@@ -473,6 +473,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
 #pragma unroll
             for (int k = 0; k < BPL; k++) nphi[k] = ax[k] = ay[k] = az[k] = splat2(0.f);
             const float2 e2 = splat2(eps2);
+#pragma unroll 2
             for (int p = 0; p < (nc + 1) >> 1; p++) {
                 const float4 P0 = S.cp[p][0], P1 = S.cp[p][1];
                 bool m0 = true, m1 = true;
