@@ -340,23 +340,27 @@ def run_ours(args, world, rank, local):
     idx = np.sort(rng.choice(n, size=min(args.sample, n), replace=False)).astype(np.int64)
     ea, _ = ctx.direct_sample(idx)
 
-    # ---- the learned criterion: labels from this system, training on the device ----
+    # ---- calibration to equal RMS (untimed): the fixed-theta rule, then the error rule ----
+    fixed = point(ctx, ("body", TOL), idx, ea)
+    target = fixed["rms"]
+    err_pt, cal_err = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, target)
+
+    # ---- the learned criterion: labels from this system, training on the device, at the
+    #      error rule's equal-RMS budget unless --train-theta names one ----
     t0 = time.perf_counter()
     set_mode(ctx, ("body", TOL))
-    ctx.evaluate()
+    ctx.evaluate()                           # accelerations of the reference rule for a_min
     tg = TUNING["group"]                     # labels from the groups the learned walk uses
     ctx.set_tuning(tg["group_max"], tg["list_depth"], tg["grouping"])
-    train = ctx.learn_from_self(theta=args.train_theta, target=1 << 20, band=tuple(args.train_band))
+    theta_train = args.train_theta if args.train_theta else (err_pt["mode"][1] if err_pt else 0.03)
+    train = ctx.learn_from_self(theta=theta_train, target=1 << 20, band=tuple(args.train_band))
     torch.cuda.synchronize()
     train["seconds"] = time.perf_counter() - t0
+    train["theta"] = theta_train
     train["band"] = list(args.band)
     ctx.learn_band(*args.band)
 
-    # ---- calibration to equal RMS (untimed) ----
-    fixed = point(ctx, ("body", TOL), idx, ea)
-    target = fixed["rms"]
     learned_mode = lambda e: ("learned", e, LEARNED_THRESHOLD)
-    err_pt, cal_err = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, target)
     lrn_pt, cal_lrn = calibrate(ctx, idx, ea, learned_mode, 1e-3, 64.0, target)
     tc1_pt, cal_tc1 = calibrate(ctx, idx, ea, lambda t: ("barnes", t), 0.3, 1.5, target, geometric=False)
     th_pt2, cal_th = calibrate(ctx, idx, ea, lambda t: ("body", t), TOL, 1.2, RMS_BUDGET, geometric=False)
@@ -605,7 +609,7 @@ def run_galaxy(args, world, rank, local):
     ea, _ = ctx.direct_sample(idx)
     tg = TUNING["group"]                     # labels from the groups the learned walk uses
     ctx.set_tuning(tg["group_max"], tg["list_depth"], tg["grouping"])
-    train = ctx.learn_from_self(theta=args.train_theta, target=1 << 20, band=tuple(args.train_band))
+    train = ctx.learn_from_self(theta=args.train_theta or 0.03, target=1 << 20, band=tuple(args.train_band))
     ctx.learn_band(*args.band)
     fixed = point(ctx, ("body", TOL), idx, ea)
     lrn_pt, cal = calibrate(ctx, idx, ea, lambda e: ("learned", e, LEARNED_THRESHOLD), 1e-3, 64.0, fixed["rms"],
@@ -700,7 +704,8 @@ def main():
                     help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
                          "ensemble: 4096 independent systems; galaxy: 2^24-body disk galaxy, leapfrog")
     ap.add_argument("--nsys", type=int, default=ENS_NSYS)
-    ap.add_argument("--train-theta", type=float, default=0.03, help="learned criterion: error budget of the label walk")
+    ap.add_argument("--train-theta", type=float, default=0.0,
+                    help="learned criterion: error budget of the label walk (default: the error rule's equal-RMS budget)")
     ap.add_argument("--train-band", type=float, nargs=2, default=[1.0, 16.0],
                     help="learned criterion: proxy band (x budget) sampled for training")
     ap.add_argument("--band", type=float, nargs=2, default=[0.5, 16.0],
