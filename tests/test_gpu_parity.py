@@ -113,6 +113,35 @@ def test_forces_at_test_points(hc, quad):
     assert ok.mean() >= FRACTION
 
 
+@pytest.mark.parametrize("kind", ["plummer200003", "cluster60000"])
+def test_large_tree_bit_exact_vs_oracle(hc, oracle_lib, kind):
+    """Trees of many sort tiles (4096 keys each, the last one ragged) against
+    the oracle's maketree/hackcofm: a Plummer sphere of 200,003 bodies, and
+    60,000 bodies of which half sit in a cluster of radius 1e-5 (a tree 29
+    levels deep, high key digits shared by half the bodies)."""
+    O = oracle_lib
+    if kind == "plummer200003":
+        m, ph = O.mkplummer(200003, 5)
+        pos = ph[:, 0].copy()
+    else:
+        rng = np.random.default_rng(17)
+        pos = rng.normal(0.0, 1.0, (60000, 3))
+        pos[::2] = 0.3 + rng.normal(0.0, 1e-5, (30000, 3))
+        m = np.full(len(pos), 1.0 / len(pos))
+    T = O.Tree(len(m), 1.0)
+    assert T.build(m, pos, True) == 0
+    ref = _canon(T.dump())
+    ph = np.zeros((len(m), 2, 3))
+    ph[:, 0] = pos
+    with hc.Context(len(m), tol=0.6, eps=0.01, fcells=1.0, usequad=True) as ctx:
+        ctx.upload(m, ph)
+        ctx.build_tree()
+        got = _canon(ctx.dump_tree())
+    assert len(got["level"]) == len(ref["level"])
+    for f in ("level", "corner", "count", "mass", "cm"):
+        assert np.array_equal(got[f], ref[f]), f
+
+
 def test_expansion_chain_and_massless(hc, oracle_lib):
     """One-body expansion cells (load.c:74-93) and massless test bodies."""
     O = oracle_lib
