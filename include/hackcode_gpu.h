@@ -159,7 +159,8 @@ int hc_last_timing(hc_ctx *ctx, double *build_ms, double *walk_ms, int64_t *laun
  * HC_CRITERION_BODY  (default): the reference's rule, per body -- open iff
  *     tol^2 |cm - x|^2 < size^2 (subdivp, grav.c:122-131); interaction sets
  *     identical to hackcode1's.
- * HC_CRITERION_GROUP: one decision per 32-body group -- open iff
+ * HC_CRITERION_GROUP: one decision per group (a tree cell of up to 64 bodies,
+ *     see hc_tuning) -- open iff
  *     theta^2 dmin^2 < size^2, dmin the distance from the group's bounding box
  *     to the cell's centre of mass (a group walk in the manner of treecode1's
  *     walktree, treegrav.c:380-419).  No counterpart in hackcode1. */
@@ -231,11 +232,11 @@ int hc_learn_relabel(hc_ctx *ctx, double rel_threshold);
  * [-lo, hi] (defaults 1 and 3); below it the cell is accepted, above opened */
 int hc_learn_set_band(hc_ctx *ctx, double lo, double hi);
 
-/* How the walk groups its 32 bodies per warp: HC_GROUPS_CONSECUTIVE (32
- * bodies consecutive in key order) or HC_GROUPS_TREE (the bodies of one cell
- * holding at most 32, siblings packed).  The interaction sets of
- * HC_CRITERION_BODY do not depend on it (the rounding of the FP32 sums does);
- * the other criteria always use tree groups. */
+/* How the per-body rule groups the bodies of a warp: HC_GROUPS_CONSECUTIVE
+ * (32 bodies consecutive in key order) or HC_GROUPS_TREE (the bodies of one
+ * cell holding at most 32, siblings packed).  Its interaction sets do not
+ * depend on it (the rounding of the FP32 sums does).  The other criteria
+ * always walk tree groups of up to 64 bodies (two per lane). */
 enum { HC_GROUPS_CONSECUTIVE = 0, HC_GROUPS_TREE = 1 };
 int hc_set_grouping(hc_ctx *ctx, int kind);
 

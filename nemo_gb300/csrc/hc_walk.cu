@@ -9,10 +9,13 @@
 // added by gravsub (Plummer-softened monopole, plus the quadrupole term in the
 // QUADPOLE build).
 //
-// Here one warp walks for a group of 32 bodies that are consecutive in Morton
-// order (a compact patch of space).  Every traversal entry carries a 32-bit
-// lane mask: the bodies whose own walk reaches that node (all ancestors
-// opened for them).  Candidates are processed 32 at a time, one per lane:
+// Here one warp walks for a group of bodies: under the reference's per-body
+// rule up to 32 (one per lane) that are consecutive in Morton order (a compact
+// patch of space) or make up a small cell; under the group criteria a cell of
+// up to 64 (two per lane).  Under the per-body rule every traversal entry
+// carries a 32-bit lane mask: the bodies whose own walk reaches that node (all
+// ancestors opened for them).  Candidates are processed 32 at a time, one per
+// lane:
 //   * against the group's bounding box: accepted by all bodies in the mask,
 //     opened by all, or "mixed";
 //   * mixed candidates are re-tested per body (broadcast by shuffle); a test
@@ -23,7 +26,8 @@
 // per-warp shared-memory stack; accepted bodies and cells are appended to two
 // shared-memory interaction lists with their accept masks, and each list is
 // evaluated by all 32 lanes when it fills (broadcast shared-memory reads,
-// FP32 FMA, rsqrt), lanes outside an entry's mask contributing zero.
+// packed FP32x2 arithmetic over two entries at a time, rsqrt), lanes outside
+// an entry's mask contributing zero.
 //
 // Precision: positions are taken relative to the group centre (FP64 centre,
 // node centres stored as FP32 hi/lo pairs), the interaction arithmetic is
@@ -92,7 +96,8 @@ struct WalkArgs {
     float eps_acc;                        // MODE 2/3 error budget relative to |a|
     const double *pax, *pay, *paz;        // MODE 2/3: accelerations of the previous evaluation
     const int *run_flag;                  // when set: the walk runs only if *run_flag != 0
-    int flush_at;                         // lists are evaluated once they hold more entries (<= 32)
+    int flush_at;                         // lists are evaluated once they hold more entries (<= 32;
+                                          // one iteration appends at most 32)
     const float *rcrit2;                  // MODE 1, treecode1 criteria: accept iff dmin^2 > rcrit2[node]
     const int32_t *sys_root, *body_sys;   // forest: root cell of each group's system
     const MlpSmem *mlp;                   // MODE 3: packed network

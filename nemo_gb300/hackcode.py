@@ -315,14 +315,15 @@ class Context:
         self._check(self._L.hc_forces(self._h))
 
     def set_criterion(self, criterion: str = "body", theta: float = 0.0):
-        """'body' (the reference's per-body rule), or one decision per 32-body group: 'group' (opening
+        """'body' (the reference's per-body rule), or one decision per group of up to 64 bodies: 'group' (opening
         angle theta), 'error' (truncation-error budget theta |a|), 'learned' (the network in the error
         rule's band)."""
         code = {"body": 0, "group": 1, "error": 2, "learned": 3, "bh86": 4, "sw94": 5, "barnes": 6}[criterion]
         self._check(self._L.hc_set_criterion(self._h, code, float(theta)))
 
     def set_grouping(self, kind: str = "consecutive"):
-        """Walk groups: 'consecutive' (32 bodies in key order) or 'tree' (cells of <= 32 bodies)."""
+        """Walk groups of the per-body rule: 'consecutive' (32 bodies in key order) or 'tree' (cells of
+        <= 32 bodies); the other criteria always walk tree groups of up to 64."""
         self._check(self._L.hc_set_grouping(self._h, {"consecutive": 0, "tree": 1}[kind]))
 
     def set_extpot(self, name=None, pars=()):
