@@ -82,6 +82,9 @@ void free_all(hc_ctx *c)
     if (c->h_box) cudaFreeHost(c->h_box);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -278,6 +281,12 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
     }
     for (auto &e : c->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return HC_ERR_CUDA;
+    if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        c->err = "cudaStreamCreate / cudaEventCreate failed";
+        return HC_ERR_CUDA;
+    }
     int r = alloc_all(c);
     if (r != HC_OK) return r;
     HC_CUDA(cudaMalloc((void **)&c->d_diag, 64 * sizeof(double)));
@@ -559,15 +568,30 @@ static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bo
     const unsigned rflags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     HC_CUDA(cudaMemsetAsync(c->st, 0, sizeof(hc_status), c->stream));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[0], c->stream, rflags));
-    HC_TRY(hc_tree_build(c));
+    const bool guard = c->guard_n > 0 && c->criterion != HC_CRITERION_BODY;
+    if (guard) {
+        // the guard's direct sum on the side stream, alongside the first build
+        // steps (they leave most SMs idle); joined before the upward pass
+        HC_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+        HC_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        hc_guard_direct_launch(c, c->side);
+        HC_CUDA(cudaEventRecord(c->ev_join, c->side));
+        c->join_pending = true;
+    }
+    const int rb = hc_tree_build(c);
+    if (c->join_pending) {                    // the build left before the upward pass
+        c->join_pending = false;
+        HC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    }
+    if (rb != HC_OK) return rb;
     if (c->criterion >= HC_CRITERION_BH86) hc_rcrit_launch(c, c->criterion - HC_CRITERION_BH86 + 1, c->group_theta);
     HC_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, rflags));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, rflags));
     HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
                           nstep));
-    if (c->guard_n > 0 && c->criterion != HC_CRITERION_BODY) {
-        // guard: sampled direct sum; on failure the per-body rule redoes the walk
-        hc_guard_launch(c);
+    if (guard) {
+        // compare with the walk's forces; on failure the per-body rule redoes the walk
+        hc_guard_check_launch(c);
         HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
                               nstep, &c->guard->flag, true));
     }

@@ -21,11 +21,21 @@ namespace {
 
 constexpr int GT = 256;
 
+__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
+
+// One thread per sampled body, a block per slice of the sources.  The slice
+// is staged in shared memory in pairs (both bodies' values of one quantity
+// adjacent: the operands of one packed FP32x2 instruction) and summed two
+// sources per step.  With softening the sample's own term is exactly zero (a
+// zero separation); without it (SELF) the sample skips itself explicitly.
+template <bool SELF>
 __global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *mass, const double *px,
                                                      const double *py, const double *pz, const int64_t *idx, int ns,
                                                      float eps2, int64_t slice, float4 *part)
 {
-    __shared__ float4 sh[GT], sl[GT];
+    __shared__ float4 sp[GT / 2][4];      // (hx hy) (hz m) (lx ly) (lz -), each for two sources
     const int s = blockIdx.y * GT + threadIdx.x;
     const bool valid = s < ns;
     const int64_t me = valid ? idx[s] : -1;
@@ -35,31 +45,45 @@ __global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *ma
                 zl = __double2float_rn(zd - (double)zh);
     const int64_t j0 = (int64_t)blockIdx.x * slice;
     const int64_t j1 = j0 + slice < n ? j0 + slice : n;
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    const float2 nxh = splat2(-xh), nyh = splat2(-yh), nzh = splat2(-zh);
+    const float2 nxl = splat2(-xl), nyl = splat2(-yl), nzl = splat2(-zl), e2 = splat2(eps2);
+    float2 ax = splat2(0.f), ay = ax, az = ax;
+    float *f = reinterpret_cast<float *>(sp[threadIdx.x >> 1]) + (threadIdx.x & 1);
     for (int64_t base = j0; base < j1; base += GT) {
         const int64_t j = base + threadIdx.x;
         if (j < j1) {
             const double x = px[j], y = py[j], z = pz[j];
             const float h0 = __double2float_rn(x), h1 = __double2float_rn(y), h2 = __double2float_rn(z);
-            sh[threadIdx.x] = make_float4(h0, h1, h2, __double2float_rn(mass[j]));
-            sl[threadIdx.x] = make_float4(__double2float_rn(x - (double)h0), __double2float_rn(y - (double)h1),
-                                          __double2float_rn(z - (double)h2), 0.f);
+            f[0] = h0;
+            f[2] = h1;
+            f[4] = h2;
+            f[6] = __double2float_rn(mass[j]);
+            f[8] = __double2float_rn(x - (double)h0);
+            f[10] = __double2float_rn(y - (double)h1);
+            f[12] = __double2float_rn(z - (double)h2);
+        } else {                                 // pad: massless, far away
+            f[0] = f[2] = f[4] = 1.0e4f;
+            f[6] = f[8] = f[10] = f[12] = 0.f;
         }
         __syncthreads();
         const int cnt = j1 - base < GT ? (int)(j1 - base) : GT;
-        for (int k = 0; k < cnt; k++) {
-            const float4 H = sh[k], L = sl[k];
-            const float dx = (H.x - xh) + (L.x - xl), dy = (H.y - yh) + (L.y - yl), dz = (H.z - zh) + (L.z - zl);
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-            const float rinv = rsqrtf(r2);
-            const float mr3 = (base + k == me) ? 0.f : H.w * rinv * rinv * rinv;   // self skipped
-            ax = fmaf(mr3, dx, ax);
-            ay = fmaf(mr3, dy, ay);
-            az = fmaf(mr3, dz, az);
+        const int self = SELF ? (int)(me - base) : -1;   // the sample's slot in this tile, if any
+        for (int p = 0; p < (cnt + 1) >> 1; p++) {
+            const float4 H0 = sp[p][0], H1 = sp[p][1], L0 = sp[p][2], L1 = sp[p][3];
+            const float2 dx = __fadd2_rn(__fadd2_rn(lo2(H0), nxh), __fadd2_rn(lo2(L0), nxl));
+            const float2 dy = __fadd2_rn(__fadd2_rn(hi2(H0), nyh), __fadd2_rn(hi2(L0), nyl));
+            const float2 dz = __fadd2_rn(__fadd2_rn(lo2(H1), nzh), __fadd2_rn(lo2(L1), nzl));
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+            float2 w = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+            if (SELF) w = make_float2(2 * p == self ? 0.f : w.x, 2 * p + 1 == self ? 0.f : w.y);
+            const float2 mr3 = __fmul2_rn(hi2(H1), __fmul2_rn(w, __fmul2_rn(w, w)));
+            ax = __ffma2_rn(mr3, dx, ax);
+            ay = __ffma2_rn(mr3, dy, ay);
+            az = __ffma2_rn(mr3, dz, az);
         }
         __syncthreads();
     }
-    if (valid) part[(int64_t)blockIdx.x * ns + s] = make_float4(ax, ay, az, 0.f);
+    if (valid) part[(int64_t)blockIdx.x * ns + s] = make_float4(ax.x + ax.y, ay.x + ay.y, az.x + az.y, 0.f);
 }
 
 // Per sampled body: its direct-sum acceleration (partials summed in slice
@@ -131,17 +155,46 @@ int hc_guard_slices(hc_ctx *c)
 }
 
 // No CUDA queries here: this runs inside stream capture.
-void hc_guard_launch(hc_ctx *c)
+static int guard_slices_used(const hc_ctx *c, int64_t *slice)
+{
+    const int64_t want = c->guard_narrow ? (c->guard_slices + 15) / 16 : c->guard_slices;
+    *slice = (c->n + want - 1) / want;
+    if (*slice < 1) *slice = 1;
+    return (int)((c->n + *slice - 1) / *slice);
+}
+
+// The direct sum needs only positions and masses: it can run while the tree
+// is built.  Beside the build it runs on a sixteenth of the slices (one block
+// per two SMs), leaving the latency-bound build kernels room.
+void hc_guard_direct_launch(hc_ctx *c, cudaStream_t s)
 {
     const int ns = (int)c->guard_n;
-    int64_t slice = (c->n + c->guard_slices - 1) / c->guard_slices;
-    if (slice < 1) slice = 1;
-    const int slices = (int)((c->n + slice - 1) / slice);
+    int64_t slice;
+    const int slices = guard_slices_used(c, &slice);
     const dim3 grid((unsigned)slices, (unsigned)((ns + GT - 1) / GT));
-    k_guard_direct<<<grid, GT, 0, c->stream>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns,
-                                              (float)(c->prm.eps * c->prm.eps), slice, c->guard_part);
+    const float eps2 = (float)(c->prm.eps * c->prm.eps);
+    if (eps2 > 0.f)
+        k_guard_direct<false><<<grid, GT, 0, s>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns, eps2, slice,
+                                                   c->guard_part);
+    else
+        k_guard_direct<true><<<grid, GT, 0, s>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns, eps2, slice,
+                                                  c->guard_part);
+    c->launches++;
+}
+
+void hc_guard_check_launch(hc_ctx *c)
+{
+    const int ns = (int)c->guard_n;
+    int64_t slice;
+    const int slices = guard_slices_used(c, &slice);
     double *rel2 = reinterpret_cast<double *>(c->guard_part + (int64_t)c->guard_slices * ns);
     k_guard_rel<<<ns, 128, 0, c->stream>>>(c->guard_part, slices, ns, c->guard_idx, c->ax, c->ay, c->az, rel2);
     k_guard_check<<<1, GT, 0, c->stream>>>(rel2, ns, c->guard_rms_max, c->guard, c->st);
-    c->launches += 3;
+    c->launches += 2;
+}
+
+void hc_guard_launch(hc_ctx *c)
+{
+    hc_guard_direct_launch(c, c->stream);
+    hc_guard_check_launch(c);
 }

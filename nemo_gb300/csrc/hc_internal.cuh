@@ -70,6 +70,10 @@ struct hc_ctx {
     int64_t maxcell;          // (int)(fcells * n), load.c:50
     hc_params prm;
     cudaStream_t stream;
+    cudaStream_t side;        // the guard's direct sum, forked from stream, joined before the upward pass
+    cudaEvent_t ev_fork, ev_join;
+    bool join_pending;        // the build waits on ev_join before the upward pass
+    bool guard_narrow;        // the guard's direct sum runs beside the build on fewer blocks
     cudaEvent_t ev[6];        // 0-1 build, 2-3 walk, 4-5 user timer
     std::string err;
     bool have_tree, have_forces;
@@ -213,6 +217,10 @@ void hc_rcrit_launch(hc_ctx *c, int kind, double theta);
 // guard (hc_guard.cu)
 int hc_guard_slices(hc_ctx *c);
 void hc_guard_launch(hc_ctx *c);
+// the guard in two parts: the sampled direct sum (on any stream), then the
+// comparison with the walk's forces and the check (on c->stream)
+void hc_guard_direct_launch(hc_ctx *c, cudaStream_t s);
+void hc_guard_check_launch(hc_ctx *c);
 int hc_fma_peak_impl(hc_ctx *c, double *tflops);
 
 #define HC_CUDA(call)                                                               \

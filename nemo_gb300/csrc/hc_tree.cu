@@ -904,7 +904,12 @@ int hc_tree_build(hc_ctx *c)
     c->launches += 7;
 
     // 6. upward pass, deepest level first, one cooperative launch, over the
-    // cells grouped by depth and child count
+    // cells grouped by depth and child count.  Work forked onto the side
+    // stream joins here: nothing else runs beside the cooperative launch.
+    if (c->join_pending) {
+        c->join_pending = false;
+        HC_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+    }
     HC_CUDA(cudaMemsetAsync(c->cbins, 0, sizeof(uint32_t) * 520, s));
     k_cell_count<<<Gn, B, 0, s>>>(c->nodeC, c->box, c->cbins);
     k_cell_offsets<<<1, 256, 0, s>>>(c->cbins, c->cbins + 260);
