@@ -264,6 +264,9 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
 {
     if (!out || nbody < 1 || !params) return HC_ERR_ARG;
     if (nbody > (1LL << 28)) return HC_ERR_ARG;
+    // bodies + cells must stay below 2^30: the radix sort's look-back words
+    // carry 30-bit counts
+    if ((double)nbody * (1.0 + std::max(params->fcells, 0.0)) >= (double)(1LL << 30)) return HC_ERR_ARG;
     hc_ctx_ext *c = new hc_ctx_ext();   // value-initialised: all pointers null
     c->n = nbody;
     c->prm = *params;
