@@ -699,7 +699,6 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=2048)
     ap.add_argument("--ref-sample", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--stats", action="store_true", help="one extra counting walk: mask popcount histogram")
     ap.add_argument("--workload", default="plummer", choices=["plummer", "hernquist", "ensemble", "galaxy"],
                     help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
                          "ensemble: 4096 independent systems; galaxy: 2^24-body disk galaxy, leapfrog")
