@@ -1,7 +1,8 @@
 """GPU edge cases of the additions: ensembles that are all-direct, all-tree or
 a single system, the rejection of massless ensemble bodies, caller-order
-independence of ensemble results, and the approximate criteria and the guard
-without quadrupoles."""
+independence of ensemble results, the approximate criteria and the guard
+without quadrupoles, test points under a group criterion, and the guard with
+CUDA graphs off."""
 import numpy as np
 import pytest
 
@@ -136,3 +137,53 @@ def test_learned_without_quadrupoles(hc):
     rms = np.sqrt(np.mean(_rel(acc[idx], ea) ** 2))
     assert rms < 3e-3, rms
     assert ctx.walk_stats()["network"] > 0
+
+
+def test_test_points_under_group_criteria(hc):
+    """hackforce's test= path (hc_forces_at: groups of 64 consecutive test
+    points, no self term) under the error rule agrees with the per-body rule
+    to the criteria's accuracy, and with an FP64 direct sum."""
+    n = 65536
+    m, ph = hc.mkplummer(n, 12)
+    rng = np.random.default_rng(5)
+    tp = rng.normal(0.0, 0.7, (5000, 3))
+    ctx = hc.Context(n, tol=0.4, eps=0.01, usequad=True)
+    ctx.upload(m, ph)
+    ctx.evaluate()
+    ab, pb = ctx.forces_at(tp)
+    ctx.set_criterion("error", 0.01)
+    ctx.evaluate()
+    ae, pe = ctx.forces_at(tp)
+    rel = _rel(ae, ab)
+    assert np.sqrt(np.mean(rel ** 2)) < 2e-3 and np.quantile(rel, 0.999) < 2e-2, (np.sqrt(np.mean(rel ** 2)),)
+    assert np.max(np.abs(pe / pb - 1)) < 1e-3
+    # direct sum for a few points
+    x = ph[:, 0]
+    for j in range(0, 5000, 997):
+        d = x - tp[j]
+        r2 = (d ** 2).sum(1) + 0.01 ** 2
+        a = (m[:, None] * d / r2[:, None] ** 1.5).sum(0)
+        assert np.linalg.norm(ae[j] - a) / np.linalg.norm(a) < 1e-2
+
+
+def test_guard_without_graphs(hc):
+    """The guard's direct sum on its side stream, with CUDA graphs off (plain
+    launches on two streams): the same statistics and forces as with graphs."""
+    n = 131072
+    m, ph = hc.mkplummer(n, 13)
+    out = {}
+    for graphs in (True, False):
+        ctx = hc.Context(n, tol=0.5, eps=0.01, usequad=True)
+        ctx.set_graphs(graphs)
+        ctx.upload(m, ph)
+        ctx.evaluate()
+        ctx.set_criterion("error", 0.03)
+        ctx.set_guard(256, 1e-2, seed=4)
+        for _ in range(3):
+            ctx.evaluate()
+        _, a, _ = ctx.download(phase=False, phi=False)
+        out[graphs] = (a, ctx.guard_stats())
+        ctx.close()
+    np.testing.assert_array_equal(out[True][0], out[False][0])
+    assert out[True][1]["checks"] == out[False][1]["checks"] == 3
+    assert out[True][1]["last_rms"] == out[False][1]["last_rms"]
