@@ -21,9 +21,6 @@ namespace {
 
 constexpr int GT = 256;
 
-__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
-__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
-__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
 
 // One thread per sampled body, a block per slice of the sources.  The slice
 // is staged in shared memory in pairs (both bodies' values of one quantity

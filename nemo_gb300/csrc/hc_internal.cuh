@@ -232,6 +232,15 @@ int hc_fma_peak_impl(hc_ctx *c, double *tflops);
         }                                                                           \
     } while (0)
 
+#ifdef __CUDACC__
+// Operands of the packed FP32x2 instructions (__ffma2_rn and relatives): a
+// float2 is one register pair.  Lists stored in pairs keep both entries'
+// values of one quantity adjacent, so lo2 / hi2 of a float4 row give them.
+__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
+#endif
+
 // Largest tree-aligned walk group of the build: up to 64 bodies when a
 // group criterion walks the tree, 32 for the per-body rule.
 static inline int hc_table_gmax(const hc_ctx *c)

@@ -202,9 +202,6 @@ __device__ __forceinline__ void two_diff(float a, float b, float &s, float &e)
 // subdivp in FP64 (grav.c:122-131): open iff tol^2 * |cm - x|^2 < dsq.
 // quantity k (0-based) of list entry e in a pair array with float4 rows
 __device__ __forceinline__ float *pair_slot(float4 *row, int e) { return reinterpret_cast<float *>(row) + (e & 1); }
-__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
-__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
-__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
 
 __device__ __forceinline__ bool open_exact(double cx, double cy, double cz, double x, double y, double z,
                                            double tol2, double dsq)
