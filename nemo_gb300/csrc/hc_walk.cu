@@ -407,6 +407,9 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
         // Body entries carry the accept mask (per-body rule) or the group slot
         // of the body that is the entry itself (group criteria; -1: none).
         const unsigned lanebit = 1u << lane;
+        // a group of at most 32 bodies has no second body on any lane: its
+        // flushes skip that half of the work (warp-uniform)
+        const bool second = BPL == 2 && cnt > 32;
         auto pad_entry = [&](float4 *row, int e, int nq) {
             float *f = pair_slot(row, e);
             f[0] = 1.0e4f;
@@ -431,6 +434,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
                 const float4 H0 = S.bp[p][0], H1 = S.bp[p][1], L0 = S.bp[p][2], L1 = S.bp[p][3];
 #pragma unroll
                 for (int k = 0; k < BPL; k++) {
+                    if (k > 0 && !second) continue;
                     const float2 dx = __fadd2_rn(__fadd2_rn(lo2(H0), splat2(-bx[k])), __fadd2_rn(lo2(L0), splat2(-blx[k])));
                     const float2 dy = __fadd2_rn(__fadd2_rn(hi2(H0), splat2(-by[k])), __fadd2_rn(hi2(L0), splat2(-bly[k])));
                     const float2 dz = __fadd2_rn(__fadd2_rn(lo2(H1), splat2(-bz[k])), __fadd2_rn(lo2(L1), splat2(-blz[k])));
@@ -493,6 +497,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
                 }
 #pragma unroll
                 for (int k = 0; k < BPL; k++) {
+                    if (k > 0 && !second) continue;
                     const float2 dx = __fadd2_rn(lo2(P0), splat2(-bx[k])), dy = __fadd2_rn(hi2(P0), splat2(-by[k])),
                                  dz = __fadd2_rn(lo2(P1), splat2(-bz[k]));
                     const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
