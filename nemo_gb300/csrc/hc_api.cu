@@ -899,7 +899,7 @@ int hc_autotune(hc_ctx *ctx, hc_tuning *best)
     std::vector<hc_tuning> cand;
     // the per-body rule walks groups of up to 32 bodies, the group criteria up to 64
     const bool body = c->criterion == HC_CRITERION_BODY;
-    const int gms_body[] = {16, 24, 32}, gms_group[] = {32, 48, 64}, lds[] = {32, 48, 64};
+    const int gms_body[] = {16, 24, 32}, gms_group[] = {HC_GROUP2 / 2, 3 * HC_GROUP2 / 4, HC_GROUP2}, lds[] = {32, 48, 64};
     for (int gm : body ? gms_body : gms_group)
         for (int ld : lds) cand.push_back(hc_tuning{gm, ld, HC_GROUPS_TREE, 0.0});
     if (c->criterion == HC_CRITERION_BODY)      // the other criteria always walk tree groups

@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
     // (bodies lane and lane + 32 on each lane: every list entry is loaded
     // once for both); the per-body rule, whose list entries carry one accept
     // bit per body, walks groups of up to 32.
-    constexpr int BPL = MODE == 0 ? 1 : 2;
+    constexpr int BPL = MODE == 0 ? 1 : HC_BPL;
     constexpr int GW = 32 * BPL;
     const int64_t nmassive = g.use_table ? g.box->nmassive : 0;
     const int64_t ng_table = g.use_table ? g.box->ngroups : 0;
@@ -407,9 +407,9 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
         // Body entries carry the accept mask (per-body rule) or the group slot
         // of the body that is the entry itself (group criteria; -1: none).
         const unsigned lanebit = 1u << lane;
-        // a group of at most 32 bodies has no second body on any lane: its
-        // flushes skip that half of the work (warp-uniform)
-        const bool second = BPL == 2 && cnt > 32;
+        // bodies k of the lanes exist only for k < ceil(cnt / 32): the flushes
+        // skip the others (warp-uniform)
+        const int nact = (int)((cnt + 31) / 32);
         auto pad_entry = [&](float4 *row, int e, int nq) {
             float *f = pair_slot(row, e);
             f[0] = 1.0e4f;
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
                 const float4 H0 = S.bp[p][0], H1 = S.bp[p][1], L0 = S.bp[p][2], L1 = S.bp[p][3];
 #pragma unroll
                 for (int k = 0; k < BPL; k++) {
-                    if (k > 0 && !second) continue;
+                    if (k > 0 && k >= nact) continue;
                     const float2 dx = __fadd2_rn(__fadd2_rn(lo2(H0), splat2(-bx[k])), __fadd2_rn(lo2(L0), splat2(-blx[k])));
                     const float2 dy = __fadd2_rn(__fadd2_rn(hi2(H0), splat2(-by[k])), __fadd2_rn(hi2(L0), splat2(-bly[k])));
                     const float2 dz = __fadd2_rn(__fadd2_rn(lo2(H1), splat2(-bz[k])), __fadd2_rn(lo2(L1), splat2(-blz[k])));
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
                 }
 #pragma unroll
                 for (int k = 0; k < BPL; k++) {
-                    if (k > 0 && !second) continue;
+                    if (k > 0 && k >= nact) continue;
                     const float2 dx = __fadd2_rn(lo2(P0), splat2(-bx[k])), dy = __fadd2_rn(hi2(P0), splat2(-by[k])),
                                  dz = __fadd2_rn(lo2(P1), splat2(-bz[k]));
                     const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
@@ -788,8 +788,8 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
 
             // ---- append accepted nodes to the interaction lists ----
             const bool ab = accm != 0u && isbody, ac = accm != 0u && !isbody;
-            // histogram of the bodies an accepted node serves, in lanes (two bodies per lane for the group criteria)
-            if (COUNT && accm != 0u) atomicAdd(&g.st->mask_hist[MODE == 0 ? __popc(accm) : (int)(cnt + 1) / 2], 1ull);
+            // histogram of the bodies an accepted node serves, in lanes (HC_BPL bodies per lane for the group criteria)
+            if (COUNT && accm != 0u) atomicAdd(&g.st->mask_hist[MODE == 0 ? __popc(accm) : (int)(cnt + BPL - 1) / BPL], 1ull);
             const unsigned bbal = __ballot_sync(FULL, ab), cbal = __ballot_sync(FULL, ac);
             if (ab) {
                 // node - centre as an unevaluated float sum hi + lo (TwoSum of the hi parts)
@@ -1096,8 +1096,8 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
     if (i >= nsample) return;
     const int grp = sample_group[i], node = sample_node[i];
     const int s0 = gstart[grp], cnt = gcount[grp];
-    // groups of up to 64 bodies: bodies lane and lane + 32 on each lane
-    constexpr int BPL = 2;
+    // groups of up to 32 HC_BPL bodies: bodies lane + 32 k on each lane
+    constexpr int BPL = HC_BPL;
     bool valid[BPL];
     uint32_t o[BPL];
     double xd[BPL], yd[BPL], zd[BPL];
@@ -1109,9 +1109,18 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
         yd[k] = py[o[k]];
         zd[k] = pz[o[k]];
     }
-    const double gx = 0.5 * (wmind(fmin(xd[0], xd[1])) + wmaxd(fmax(xd[0], xd[1]))),
-                 gy = 0.5 * (wmind(fmin(yd[0], yd[1])) + wmaxd(fmax(yd[0], yd[1]))),
-                 gz = 0.5 * (wmind(fmin(zd[0], zd[1])) + wmaxd(fmax(zd[0], zd[1])));
+    double lox = xd[0], hix = xd[0], loy = yd[0], hiy = yd[0], loz = zd[0], hiz = zd[0];
+#pragma unroll
+    for (int k = 1; k < BPL; k++) {
+        lox = fmin(lox, xd[k]);
+        hix = fmax(hix, xd[k]);
+        loy = fmin(loy, yd[k]);
+        hiy = fmax(hiy, yd[k]);
+        loz = fmin(loz, zd[k]);
+        hiz = fmax(hiz, zd[k]);
+    }
+    const double gx = 0.5 * (wmind(lox) + wmaxd(hix)), gy = 0.5 * (wmind(loy) + wmaxd(hiy)),
+                 gz = 0.5 * (wmind(loz) + wmaxd(hiz));
     const float ghx = __double2float_rn(gx), ghy = __double2float_rn(gy), ghz = __double2float_rn(gz);
     const float glx = __double2float_rn(gx - (double)ghx), gly = __double2float_rn(gy - (double)ghy),
                 glz = __double2float_rn(gz - (double)ghz);
@@ -1124,9 +1133,18 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
         const uint32_t q = o[k];
         amag[k] = (float)sqrt(ax[q] * ax[q] + ay[q] * ay[q] + az[q] * az[q]);
     }
-    const float gminx = wmin(fminf(bx[0], bx[1])), gmaxx = wmax(fmaxf(bx[0], bx[1])),
-                gminy = wmin(fminf(by[0], by[1])), gmaxy = wmax(fmaxf(by[0], by[1])),
-                gminz = wmin(fminf(bz[0], bz[1])), gmaxz = wmax(fmaxf(bz[0], bz[1]));
+    float mnx = bx[0], mxx = bx[0], mny = by[0], mxy = by[0], mnz = bz[0], mxz = bz[0];
+#pragma unroll
+    for (int k = 1; k < BPL; k++) {
+        mnx = fminf(mnx, bx[k]);
+        mxx = fmaxf(mxx, bx[k]);
+        mny = fminf(mny, by[k]);
+        mxy = fmaxf(mxy, by[k]);
+        mnz = fminf(mnz, bz[k]);
+        mxz = fmaxf(mxz, bz[k]);
+    }
+    const float gminx = wmin(mnx), gmaxx = wmax(mxx), gminy = wmin(mny), gmaxy = wmax(mxy), gminz = wmin(mnz),
+                gmaxz = wmax(mxz);
     const float eps2 = g.eps2f;
     auto rel_pos = [&](int k, float &cx, float &cy, float &cz) {
         const float4 A = g.nodeA[k], B = g.nodeB[k];
