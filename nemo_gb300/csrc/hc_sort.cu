@@ -4,8 +4,10 @@
 // GB300 build instead sorts all bodies by their 90-bit integer-coordinate key
 // (top 63 bits radix sorted, the low 27 bits resolved inside runs of equal
 // high keys), so that every octree cell is a contiguous run of sorted bodies.
-// Both kernels here are HBM-bound integer work: coalesced tile loads, block-
-// local histograms in shared memory, stable scatter.
+// Integer work with little arithmetic: coalesced tile loads, block-local
+// histograms and ranks in shared memory, a stable scatter staged in digit
+// order.  At N=1M each sort pass moves 32 MB (5 us at HBM rate) and is bound
+// by latency instead (about 20 us per pass).
 #include <algorithm>
 #include "hc_internal.cuh"
 
