@@ -20,9 +20,9 @@
 #define HC_IMAX (1 << 30)     // defs.h:124-128
 #define HC_MAXLEVEL 31        // levels 0..30
 #define HC_GROUP 32           // bodies per walk group of the per-body rule (one warp, one body per lane)
-#define HC_BPL 2              // bodies per lane of the group criteria's walk (3, with groups of up to
-                              // 96, was measured: the wider groups' deeper traversal stacks fall into
-                              // one-candidate-per-iteration steps and the walk ran 50 times longer)
+#define HC_BPL 2              // bodies per lane of the group criteria's walk (3 was measured: 6% slower
+                              // with 64-body groups, and groups of more than 64 bodies ran 50 times
+                              // longer for a reason not yet found; not used)
 #define HC_GROUP2 (32 * HC_BPL)  // bodies per walk group of the group criteria
 
 // Device status word (written by kernels, read by the host after a sync).

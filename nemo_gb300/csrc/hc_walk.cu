@@ -587,10 +587,12 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
                 }
             }
             // ---- gather up to 32 candidates from the top of the stack ----
-            // Near the stack's capacity take one node at a time: an iteration
-            // then adds at most one entry, so the stack stays within capacity
-            // for any tree depth (32 candidates that all open add up to 28).
-            const int gmax = sp > STACK - 40 ? 1 : 32;
+            // Each candidate taken adds at most one entry (its child range), so
+            // taking at most half the free entries keeps the stack within
+            // capacity; near it the walk takes fewer candidates per iteration,
+            // down to one, instead of dropping to one at a fixed threshold.
+            const int gfree = (STACK - sp) / 2;
+            const int gmax = gfree >= 32 ? 32 : (gfree >= 1 ? gfree : 1);
             while (!mlp_round && ncand < gmax && sp > 0) {
                 const uint2 e = S.stack[sp - 1];
                 const int start = (int)(e.x >> 3), ecnt = (int)(e.x & 7u) + 1;
