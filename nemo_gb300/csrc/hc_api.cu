@@ -69,7 +69,7 @@ void free_all(hc_ctx *c)
                     c->nodeA, c->nodeB, c->nodeQ, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->flags,
                     c->scan_tmp, c->hist, c->cand, c->ncand, c->diag_part, c->st, c->box, c->tx, c->ty, c->tz,
                     c->tax, c->tay, c->taz, c->tphi, c->tkhi[0], c->tkhi[1], c->tklo[0], c->tklo[1],
-                    c->tkval[0], c->tkval[1]};
+                    c->tkval[0], c->tkval[1], c->thist};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     void *mptrs[] = {c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_grad, c->mlp_loss, c->mlp_gpart, c->mlp_lpart,
@@ -163,13 +163,21 @@ int alloc_all(hc_ctx *c)
     return HC_OK;
 }
 
+// Test-point buffers, grown on demand.  Their sort has its own scratch
+// (thist): the tree's (hist) is baked into captured graphs and never moves.
+// A failed allocation leaves the buffers null and the capacity 0.
 int ensure_test_capacity(hc_ctx *c, int64_t nt)
 {
     if (nt <= c->tcap) return HC_OK;
-    void *ptrs[] = {c->tx, c->ty, c->tz, c->tax, c->tay, c->taz, c->tphi, c->tkhi[0], c->tkhi[1],
-                    c->tklo[0], c->tklo[1], c->tkval[0], c->tkval[1]};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    c->tcap = 0;
+    void **ptrs[] = {(void **)&c->tx, (void **)&c->ty, (void **)&c->tz, (void **)&c->tax, (void **)&c->tay,
+                     (void **)&c->taz, (void **)&c->tphi, (void **)&c->tkhi[0], (void **)&c->tkhi[1],
+                     (void **)&c->tklo[0], (void **)&c->tklo[1], (void **)&c->tkval[0], (void **)&c->tkval[1],
+                     (void **)&c->thist};
+    for (void **p : ptrs) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
     double **dd[] = {&c->tx, &c->ty, &c->tz, &c->tax, &c->tay, &c->taz, &c->tphi};
     for (double **p : dd) HC_TRY(dalloc(c, p, nt));
     for (int i = 0; i < 2; i++) {
@@ -177,11 +185,7 @@ int ensure_test_capacity(hc_ctx *c, int64_t nt)
         HC_TRY(dalloc(c, &c->tklo[i], nt));
         HC_TRY(dalloc(c, &c->tkval[i], nt));
     }
-    // the radix sort histograms are sized for max(n, maxnode); grow if needed
-    if (nt > std::max<int64_t>(c->n, c->maxnode)) {
-        cudaFree(c->hist);
-        HC_TRY(dalloc(c, &c->hist, hc_sort_scratch_words(nt)));
-    }
+    HC_TRY(dalloc(c, &c->thist, hc_sort_scratch_words(nt)));
     c->tcap = nt;
     return HC_OK;
 }
@@ -481,7 +485,7 @@ int hc_forces_at(hc_ctx *ctx, const double *test_pos, int64_t ntest, double *acc
     HC_CUDA(cudaMemcpyAsync(c->stage.d, test_pos, sizeof(double) * 3 * ntest, cudaMemcpyHostToDevice, c->stream));
     k_unpack3<<<hc_grid(ntest, 256), 256, 0, c->stream>>>(c->stage.d, ntest, c->tx, c->ty, c->tz);
     hc_keys_for_points(c, c->tx, c->ty, c->tz, ntest, c->tkhi[0], c->tklo[0], c->tkval[0]);
-    int sel = hc_radix_sort_keys(c, c->tkhi, c->tklo, c->tkval, ntest, 0, 64, false);
+    int sel = hc_radix_sort_keys(c, c->thist, c->tkhi, c->tklo, c->tkval, ntest, 0, 64, false);
     HC_CUDA(cudaEventRecord(c->ev[2], c->stream));
     HC_TRY(hc_walk_launch(c, false, ntest, c->tkval[sel], c->tx, c->ty, c->tz, c->tax, c->tay, c->taz, c->tphi,
                           0.0, 0));

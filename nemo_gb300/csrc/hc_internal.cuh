@@ -178,16 +178,19 @@ struct hc_ctx {
     double *tx, *ty, *tz, *tax, *tay, *taz, *tphi;
     unsigned long long *tkhi[2];
     uint32_t *tklo[2], *tkval[2];
+    uint32_t *thist;          // their radix sort's scratch (hist is baked into captured graphs)
 };
 
 // ---- host-side launchers implemented in the .cu files ----
 // scan / sort (hc_sort.cu)
 void hc_scan_exclusive_i32(hc_ctx *c, const int32_t *in, int32_t *out, int64_t n, int32_t *total_dev);
-// 32-bit words of sort scratch (c->hist) for sorting n keys (n < 2^30)
+// 32-bit words of sort scratch for sorting n keys (n < 2^30)
 int64_t hc_sort_scratch_words(int64_t n);
 int hc_sort_setup(hc_ctx *c);
-int hc_radix_sort_keys(hc_ctx *c, unsigned long long *khi[2], uint32_t *klo[2], uint32_t *kval[2],
-                       int64_t n, int begin_bit, int end_bit, bool tie_fix, const int *n_dev = nullptr);
+// scratch: hc_sort_scratch_words(n) words (c->hist for the tree, c->thist for test points)
+int hc_radix_sort_keys(hc_ctx *c, uint32_t *scratch, unsigned long long *khi[2], uint32_t *klo[2],
+                       uint32_t *kval[2], int64_t n, int begin_bit, int end_bit, bool tie_fix,
+                       const int *n_dev = nullptr);
 // tree (hc_tree.cu)
 int hc_tree_build(hc_ctx *c);
 int hc_tree_setup(hc_ctx *c);

@@ -346,18 +346,18 @@ int64_t hc_sort_scratch_words(int64_t n)
     return 4096 + (int64_t)NPASS_MAX * 256 * (ntiles < 1 ? 1 : ntiles);
 }
 
-int hc_radix_sort_keys(hc_ctx *c, unsigned long long *khi[2], uint32_t *klo[2], uint32_t *kval[2],
-                       int64_t n, int begin_bit, int end_bit, bool tie_fix, const int *n_dev)
+int hc_radix_sort_keys(hc_ctx *c, uint32_t *scratch, unsigned long long *khi[2], uint32_t *klo[2],
+                       uint32_t *kval[2], int64_t n, int begin_bit, int end_bit, bool tie_fix, const int *n_dev)
 {
     int sel = 0;
     if (n <= 0) return sel;
     const int npass = (end_bit - begin_bit + 7) / 8;
     const int64_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
-    // scratch (c->hist): [0, 2048) digit counts -> offsets per pass (left there:
-    // the depth sort's offsets are the tree's level starts), [2048, 2056)
-    // tile counters, [4096, ...) look-back words, ntiles x 256 per pass
-    uint32_t *ghist = c->hist, *ctr = c->hist + 2048, *look = c->hist + 4096;
-    cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * (4096 + (size_t)npass * 256 * ntiles), c->stream);
+    // scratch: [0, 2048) digit counts -> offsets per pass (left there: the
+    // depth sort's offsets are the tree's level starts), [2048, 2056) tile
+    // counters, [4096, ...) look-back words, ntiles x 256 per pass
+    uint32_t *ghist = scratch, *ctr = scratch + 2048, *look = scratch + 4096;
+    cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * (4096 + (size_t)npass * 256 * ntiles), c->stream);
     const int hblocks = (int)std::min<int64_t>((n + SORT_TILE - 1) / SORT_TILE, 152 * 8);
     k_sort_hist<<<hblocks < 1 ? 1 : hblocks, SORT_THREADS, 0, c->stream>>>(khi[sel], n, n_dev, begin_bit, npass,
                                                                           ghist);

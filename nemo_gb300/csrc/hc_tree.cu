@@ -864,7 +864,7 @@ int hc_tree_build(hc_ctx *c)
 
     // 2-3. keys, sort, massive compaction
     hc_keys_for_points(c, c->px, c->py, c->pz, n, c->khi[0], c->klo[0], c->kval[0]);
-    int sel = hc_radix_sort_keys(c, c->khi, c->klo, c->kval, n, 0, 64, true);
+    int sel = hc_radix_sort_keys(c, c->hist, c->khi, c->klo, c->kval, n, 0, 64, true);
     c->sort_sel = sel;
     c->sidx = c->kval[sel];
     int32_t *sflag = c->flags;            // reuse (outside no longer needed)
@@ -891,7 +891,7 @@ int hc_tree_build(hc_ctx *c)
 
     // 5. breadth-first layout: stable sort of the pre-order by depth (count on the device)
     uint32_t *nolo[2] = {nullptr, nullptr};
-    int dsel = hc_radix_sort_keys(c, c->dkey, nolo, c->dval, c->maxnode, 0, 8, false, &c->box->nnode);
+    int dsel = hc_radix_sort_keys(c, c->hist, c->dkey, nolo, c->dval, c->maxnode, 0, 8, false, &c->box->nnode);
     c->bfs2pre = c->dval[dsel];
     k_levels<<<1, 64, 0, s>>>(c->hist, c->box);      // the sort leaves its digit offsets at hist[0..255]
     k_pre2bfs<<<Gn, B, 0, s>>>(c->bfs2pre, c->box, c->pre2bfs);

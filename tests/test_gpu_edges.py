@@ -1,8 +1,8 @@
 """GPU edge cases of the additions: ensembles that are all-direct, all-tree or
 a single system, the rejection of massless ensemble bodies, caller-order
 independence of ensemble results, the approximate criteria and the guard
-without quadrupoles, test points under a group criterion, and the guard with
-CUDA graphs off."""
+without quadrupoles, test points under a group criterion, the guard with
+CUDA graphs off, and more test points than tree nodes between graph replays."""
 import numpy as np
 import pytest
 
@@ -187,3 +187,30 @@ def test_guard_without_graphs(hc):
     np.testing.assert_array_equal(out[True][0], out[False][0])
     assert out[True][1]["checks"] == out[False][1]["checks"] == 3
     assert out[True][1]["last_rms"] == out[False][1]["last_rms"]
+
+
+def test_many_test_points_keep_the_captured_graphs(hc):
+    """More test points than the context has tree nodes: their sort's scratch
+    grows on its own, so the evaluation graph captured before them (which
+    holds the tree sort's scratch) replays afterwards to the same forces, and
+    a second, smaller call reuses the grown buffers."""
+    n = 1000
+    m, ph = hc.mkplummer(n, 21)
+    rng = np.random.default_rng(8)
+    test = rng.uniform(-1.0, 1.0, (40000, 3))          # about 20 times the node capacity
+    with hc.Context(n, tol=0.6, eps=0.05, usequad=True) as ctx:
+        ctx.upload(m, ph)
+        ctx.evaluate()
+        _, a0, p0 = ctx.download(phase=False)
+        acc, phi = ctx.forces_at(test)
+        acc2, phi2 = ctx.forces_at(test[:5000])
+        ctx.upload(m, ph)
+        ctx.evaluate()
+        _, a1, p1 = ctx.download(phase=False)
+    np.testing.assert_array_equal(a0, a1)
+    np.testing.assert_array_equal(p0, p1)
+    assert np.isfinite(acc).all() and np.isfinite(phi).all()
+    # the same interaction sets; group centres differ with the test set, so
+    # the FP32 sums agree to rounding, not bit for bit
+    assert _rel(acc2, acc[:5000]).max() < 1e-5
+    assert (np.abs(phi2 - phi[:5000]) / np.abs(phi[:5000])).max() < 1e-5
