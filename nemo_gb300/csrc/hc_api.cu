@@ -237,6 +237,7 @@ int staging(hc_ctx *c, Staging &s, int64_t count)
     if (count <= s.cap) return HC_OK;
     if (s.d) cudaFree(s.d);
     s.d = nullptr;
+    s.cap = 0;
     HC_TRY(dalloc(c, &s.d, count));
     s.cap = count;
     return HC_OK;
@@ -721,6 +722,7 @@ int hc_direct_sample(hc_ctx *ctx, const int64_t *index, int64_t ns, double *acc,
         if (c->d_out) cudaFree(c->d_out);
         c->d_idx = nullptr;
         c->d_out = nullptr;
+        c->idx_cap = 0;
         HC_TRY(dalloc(c, &c->d_idx, ns));
         HC_TRY(dalloc(c, &c->d_out, 4 * ns));
         c->idx_cap = ns;
@@ -944,10 +946,14 @@ int hc_set_grouping(hc_ctx *ctx, int kind)
 static int ensure_samples(hc_ctx *c, int64_t cap)
 {
     if (cap <= c->sample_capacity) return HC_OK;
-    void *ptrs[] = {c->sample_x, c->sample_amin, c->sample_y, c->sample_rel, c->sample_w, c->sample_group,
-                    c->sample_node};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    c->sample_capacity = 0;          // a failed allocation leaves the buffers null
+    void **ptrs[] = {(void **)&c->sample_x, (void **)&c->sample_amin, (void **)&c->sample_y,
+                     (void **)&c->sample_rel, (void **)&c->sample_w, (void **)&c->sample_group,
+                     (void **)&c->sample_node};
+    for (void **p : ptrs) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
     HC_TRY(dalloc(c, &c->sample_x, 12 * cap));
     HC_TRY(dalloc(c, &c->sample_amin, cap));
     HC_TRY(dalloc(c, &c->sample_y, cap));
