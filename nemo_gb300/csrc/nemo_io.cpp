@@ -370,6 +370,7 @@ bool Reader::read_item(Item &it)
             if (fread(&d, sizeof d, 1, f_) != 1) throw std::runtime_error("gethdr: EOF reading dimensions");
             if (swap_) bswap(&d, sizeof d, 1);
             if (d == 0) break;
+            if (d < 0) throw std::runtime_error("gethdr: negative dimension " + std::to_string(d));
             it.dims.push_back(d);
         }
     }
@@ -439,7 +440,9 @@ bool read_snapshot(Reader &r, Snapshot &s, std::vector<std::string> *history, st
         s.nbody = as_int(*nobj);
         if (s.nbody < 1) throw std::runtime_error("read_snapshot: Nobj = " + std::to_string(s.nbody) + " is absurd");
         if (const Item *t = par->find("Time")) {
-            s.time = as_doubles(*t)[0];
+            const std::vector<double> tv = as_doubles(*t);
+            if (tv.empty()) throw std::runtime_error("read_snapshot: Time is empty");
+            s.time = tv[0];
             s.bits |= TimeBit;
         }
         if (const Item *cs = pts->find("CoordSystem"))
@@ -455,6 +458,8 @@ bool read_snapshot(Reader &r, Snapshot &s, std::vector<std::string> *history, st
             s.bits |= PhaseSpaceBit;
         } else if (pts->find("Position") && pts->find("Velocity")) {
             std::vector<double> x = as_doubles(*pts->find("Position")), v = as_doubles(*pts->find("Velocity"));
+            if (x.size() != 3 * n || v.size() != 3 * n)
+                throw std::runtime_error("read_snapshot: Position or Velocity has wrong length");
             s.phase.resize(6 * n);
             for (size_t i = 0; i < n; i++)
                 for (int k = 0; k < 3; k++) {
@@ -474,6 +479,10 @@ bool read_snapshot(Reader &r, Snapshot &s, std::vector<std::string> *history, st
         if ((s.bits & MassBit) && s.mass.size() != n) throw std::runtime_error("read_snapshot: Mass has wrong length");
         if ((s.bits & PhaseSpaceBit) && s.phase.size() != 6 * n)
             throw std::runtime_error("read_snapshot: PhaseSpace has wrong length");
+        if ((s.bits & PotentialBit) && s.phi.size() != n)
+            throw std::runtime_error("read_snapshot: Potential has wrong length");
+        if ((s.bits & AccelerationBit) && s.acc.size() != 3 * n)
+            throw std::runtime_error("read_snapshot: Acceleration has wrong length");
         return true;
     }
     return false;
@@ -742,10 +751,11 @@ extern "C" {
 // `out` in canonical layout.  Returns the number of snapshots or -1.
 int hc_snapcopy(const char *in, const char *out)
 {
+    FILE *fi = nullptr, *fo = nullptr;
     try {
-        FILE *fi = nemo::stropen(in, "r");
+        fi = nemo::stropen(in, "r");
         nemo::Reader r(fi);
-        FILE *fo = nemo::stropen(out, "w");
+        fo = nemo::stropen(out, "w");
         nemo::Writer w(fo);
         std::vector<std::string> hist;
         std::string head;
@@ -773,6 +783,8 @@ int hc_snapcopy(const char *in, const char *out)
         nemo::strclose(fo);
         return count;
     } catch (std::exception &) {
+        nemo::strclose(fi);
+        nemo::strclose(fo);
         return -1;
     }
 }

@@ -129,6 +129,43 @@ def test_filestruct_roundtrip_through_cpp(lib, tmp_path):
     assert [x.time for x in snaps] == [0.0, 0.5] and snaps[0].phase.shape == (37, 2, 3)
 
 
+def test_malformed_snapshots_are_rejected(lib, tmp_path):
+    """Inputs get_snap refuses come back as an error, not a crash: arrays of
+    the wrong length, a negative dimension, a file cut short."""
+    from nemo_gb300 import filestruct as fs
+    n = 5
+
+    def frame(path, mass_n=n, phase_dims=(n, 2, 3), pos_n=None):
+        with open(path, "wb") as f:
+            w = fs.Writer(f)
+            w.set("SnapShot")
+            w.set("Parameters")
+            w.data("Nobj", "i", np.array(n, dtype=np.int32))
+            w.tes()
+            w.set("Particles")
+            w.data("Mass", "d", np.ones(mass_n), [mass_n])
+            if pos_n is None:
+                w.data("PhaseSpace", "d", np.zeros(6 * n), list(phase_dims))
+            else:
+                w.data("Position", "d", np.zeros(3 * pos_n), [pos_n, 3])
+                w.data("Velocity", "d", np.zeros(3 * n), [n, 3])
+            w.tes()
+            w.tes()
+
+    out = str(tmp_path / "out.snap").encode()
+    good = tmp_path / "good.snap"
+    frame(good)
+    assert lib.library().hc_snapcopy(str(good).encode(), out) == 1
+    cases = {"mass": dict(mass_n=4), "negative": dict(phase_dims=(-n, 2, 3)), "position": dict(pos_n=4)}
+    for name, kw in cases.items():
+        p = tmp_path / f"{name}.snap"
+        frame(p, **kw)
+        assert lib.library().hc_snapcopy(str(p).encode(), out) == -1, name
+    cut = tmp_path / "cut.snap"
+    cut.write_bytes(good.read_bytes()[:-40])
+    assert lib.library().hc_snapcopy(str(cut).encode(), out) == -1
+
+
 def _run(prog, *args):
     exe = os.path.join(ROOT, "nemo_gb300", "bin", prog)
     return subprocess.run([exe, *args], capture_output=True, text=True, timeout=60)
