@@ -114,13 +114,18 @@ void restorestate(Run &r, const std::string &file)
     FILE *f = stropen(file, "r");
     Reader rd(f);
     Item it;
+    auto need = [&](const Item &x, size_t bytes) {
+        if (x.data.size() < bytes) throw std::runtime_error("restorestate: item " + x.tag + " too short in " + file);
+    };
     auto getd = [&](const Item &x) {
         double v;
+        need(x, 8);
         memcpy(&v, x.data.data(), 8);
         return v;
     };
     auto geti = [&](const Item &x) {
         int v;
+        need(x, 4);
         memcpy(&v, x.data.data(), 4);
         return v;
     };
@@ -147,7 +152,10 @@ void restorestate(Run &r, const std::string &file)
         else if (t == "tout") r.tout = getd(it);
         else if (t == "minor_tout") r.minor_tout = getd(it);
         else if (t == "nstep") r.nstep = geti(it);
-        else if (t == "rmin") memcpy(r.rmin, it.data.data(), 24);
+        else if (t == "rmin") {
+            need(it, 24);
+            memcpy(r.rmin, it.data.data(), 24);
+        }
         else if (t == "rsize") r.rsize = getd(it);
         else if (t == "nbody") r.nbody = geti(it);
         else if (t == "bodytab") tab = it.data;

@@ -166,6 +166,19 @@ def test_malformed_snapshots_are_rejected(lib, tmp_path):
     assert lib.library().hc_snapcopy(str(cut).encode(), out) == -1
 
 
+def test_short_state_items_are_rejected(lib, tmp_path):
+    """restorestate with an item shorter than its type needs (a 4-byte tnow)
+    stops with hackcode1's fatal-error line before any device work."""
+    from nemo_gb300 import filestruct as fs
+    st = tmp_path / "state"
+    with open(st, "wb") as f:
+        w = fs.Writer(f)
+        w.string("program", "hackcode1")
+        w.data("tnow", "f", np.array(1.0, dtype=np.float32))
+    r = _run("hackcode1", f"restart={st}", "out=.")
+    assert r.returncode != 0 and "### Fatal error [hackcode1]" in r.stderr and "too short" in r.stderr
+
+
 def _run(prog, *args):
     exe = os.path.join(ROOT, "nemo_gb300", "bin", prog)
     return subprocess.run([exe, *args], capture_output=True, text=True, timeout=60)
