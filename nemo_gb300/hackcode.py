@@ -284,7 +284,7 @@ class Context:
         return t.value
 
     def set_box(self, rmin, rsize):
-        self._check(self._L.hc_set_box(self._h, np.ascontiguousarray(rmin, dtype=np.float64), float(rsize)))
+        self._check(self._L.hc_set_box(self._h, np.ascontiguousarray(rmin, dtype=np.float64).reshape(3), float(rsize)))
 
     def box(self):
         r = np.zeros(3)
