@@ -74,7 +74,8 @@ typedef struct {
 
 /* Create a context for nbody bodies.  Allocates all device memory once
  * (the reference allocates its cell pool once too, load.c:49-53).
- * nbody <= 2^28 and nbody * (1 + fcells) < 2^30, else HC_ERR_ARG.
+ * nbody <= 2^28, nbody * (1 + fcells) < 2^30 and finite tol, eps and fcells,
+ * else HC_ERR_ARG.
  * Replaces: startrun's allocation and box set-up, code.c:70-122. */
 int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params);
 void hc_destroy(hc_ctx *ctx);

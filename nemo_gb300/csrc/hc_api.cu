@@ -269,6 +269,8 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
 {
     if (!out || nbody < 1 || !params) return HC_ERR_ARG;
     if (nbody > (1LL << 28)) return HC_ERR_ARG;
+    if (!std::isfinite(params->tol) || !std::isfinite(params->eps) || !std::isfinite(params->fcells))
+        return HC_ERR_ARG;
     // bodies + cells must stay below 2^30: the radix sort's look-back words
     // carry 30-bit counts
     if ((double)nbody * (1.0 + std::max(params->fcells, 0.0)) >= (double)(1LL << 30)) return HC_ERR_ARG;
@@ -332,6 +334,10 @@ const char *hc_last_error(const hc_ctx *ctx) { return ctx ? ctx->err.c_str() : "
 int hc_set_params(hc_ctx *c, const hc_params *p)
 {
     if (!c || !p) return HC_ERR_ARG;
+    if (!std::isfinite(p->tol) || !std::isfinite(p->eps)) {
+        c->err = "tol and eps must be finite";
+        return HC_ERR_ARG;
+    }
     if ((int64_t)(p->fcells * (double)c->n) != c->maxcell) {
         c->err = "fcells is fixed when the context is created (load.c:49-53 allocates the cell pool once)";
         return HC_ERR_ARG;

@@ -51,6 +51,21 @@ def test_library_exports_every_declared_symbol(lib):
     assert sorted(lib.EXPORTS) == sorted(names)
 
 
+def test_create_rejects_sizes_and_parameters_out_of_range(lib):
+    """hc_create's argument checks run before any device call: more than 2^28
+    bodies, bodies + cells reaching 2^30 (the sort's 30-bit look-back counts),
+    non-finite tol / eps / fcells."""
+    import ctypes as C
+    L = lib.library()
+    bad = [(1 << 28) + 1, 1.0, 0.05, 1.0], [1 << 28, 1.0, 0.05, 3.0], [1000, float("nan"), 0.05, 1.0], \
+        [1000, 1.0, float("inf"), 1.0], [1000, 1.0, 0.05, float("nan")], [0, 1.0, 0.05, 1.0]
+    for n, tol, eps, fcells in bad:
+        h = C.c_void_p()
+        prm = lib.Params(tol, eps, fcells, 1, 0)
+        assert L.hc_create(C.byref(h), n, C.byref(prm)) == -1, (n, tol, eps, fcells)   # HC_ERR_ARG
+        assert not h.value
+
+
 def test_host_generators_match_oracle_and_pin(lib, oracle_lib):
     O = oracle_lib
     for n, seed in ((10240, 123), (777, 5)):
