@@ -388,7 +388,9 @@ int hc_set_forces(hc_ctx *ctx, const double *acc, const double *phi)
 
 int hc_set_box(hc_ctx *c, const double rmin[3], double rsize)
 {
-    if (!c || !rmin || !(rsize > 0)) return HC_ERR_ARG;
+    if (!c || !rmin || !(rsize > 0) || !std::isfinite(rsize)) return HC_ERR_ARG;
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(rmin[k])) return HC_ERR_ARG;
     HC_CUDA(cudaStreamSynchronize(c->stream));
     HC_CUDA(cudaMemcpy(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost));
     for (int k = 0; k < 3; k++) c->h_box->rmin[k] = rmin[k];
