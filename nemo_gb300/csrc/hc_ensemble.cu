@@ -457,7 +457,7 @@ int hc_ens_create(hc_ens **out, int nsys, const int64_t *counts, const hc_ens_pa
 {
     if (!out || nsys < 1 || !counts || !params) return HC_ERR_ARG;
     if (params->direct_max < 0 || params->direct_max > HC_ENS_DIRECT_LIMIT || !(params->eps >= 0.0) ||
-        !(params->tol >= 0.0))
+        !(params->tol >= 0.0) || !std::isfinite(params->eps) || !std::isfinite(params->tol))
         return HC_ERR_ARG;
     hc_ens *e = new hc_ens();
     *out = e;
@@ -468,6 +468,10 @@ int hc_ens_create(hc_ens **out, int nsys, const int64_t *counts, const hc_ens_pa
     for (int s = 0; s < nsys; s++) {
         if (counts[s] < 1) {
             e->err = "every system needs at least one body";
+            return HC_ERR_ARG;
+        }
+        if (counts[s] > (1LL << 28) || e->user_off[s] + counts[s] > (1LL << 28)) {
+            e->err = "at most 2^28 bodies in all";
             return HC_ERR_ARG;
         }
         e->user_off[s + 1] = e->user_off[s] + counts[s];

@@ -52,9 +52,9 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_create_rejects_sizes_and_parameters_out_of_range(lib):
-    """hc_create's argument checks run before any device call: more than 2^28
-    bodies, bodies + cells reaching 2^30 (the sort's 30-bit look-back counts),
-    non-finite tol / eps / fcells."""
+    """hc_create's and hc_ens_create's argument checks run before any device
+    call: more than 2^28 bodies, bodies + cells reaching 2^30 (the sort's
+    30-bit look-back counts), non-finite tol / eps / fcells, empty systems."""
     import ctypes as C
     L = lib.library()
     bad = [(1 << 28) + 1, 1.0, 0.05, 1.0], [1 << 28, 1.0, 0.05, 3.0], [1000, float("nan"), 0.05, 1.0], \
@@ -64,6 +64,10 @@ def test_create_rejects_sizes_and_parameters_out_of_range(lib):
         prm = lib.Params(tol, eps, fcells, 1, 0)
         assert L.hc_create(C.byref(h), n, C.byref(prm)) == -1, (n, tol, eps, fcells)   # HC_ERR_ARG
         assert not h.value
+    for counts, tol in (([1 << 28, 1], 0.6), ([1 << 62, 1 << 62], 0.6), ([100, 0], 0.6), ([100], float("inf"))):
+        with pytest.raises(lib.HCError) as e:
+            lib.Ensemble(counts, tol=tol)
+        assert e.value.code == -1
 
 
 def test_host_generators_match_oracle_and_pin(lib, oracle_lib):
