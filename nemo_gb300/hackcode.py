@@ -227,9 +227,11 @@ class Context:
 
     # ---- state ----
     def set_params(self, **kw):
+        p = Params.from_buffer_copy(self.params)         # kept only if the library accepts it
         for k, v in kw.items():
-            setattr(self.params, k, type(getattr(self.params, k))(v))
-        self._check(self._L.hc_set_params(self._h, C.byref(self.params)))
+            setattr(p, k, type(getattr(p, k))(v))
+        self._check(self._L.hc_set_params(self._h, C.byref(p)))
+        self.params = p
 
     def upload(self, mass, phase):
         m = np.ascontiguousarray(mass, dtype=np.float64)

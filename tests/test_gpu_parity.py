@@ -189,6 +189,16 @@ def test_errors_are_reported(hc, oracle_lib):
         with pytest.raises(hc.HCError) as e:
             ctx.forces()
         assert e.value.code == -6
+        for kw in ({"tol": float("nan")}, {"eps": float("inf")}):
+            with pytest.raises(hc.HCError) as e:
+                ctx.set_params(**kw)
+            assert e.value.code == -1
+        ctx.set_params(tol=1.0, eps=0.05)
+        for rmin, rsize in (([-2.0, -2.0, -2.0], float("inf")), ([float("nan"), -2.0, -2.0], 4.0)):
+            with pytest.raises(hc.HCError) as e:
+                ctx.set_box(rmin, rsize)
+            assert e.value.code == -1
+        ctx.build_tree()                      # the context is still usable
 
 
 def test_single_and_empty_trees(hc):
