@@ -921,11 +921,17 @@ int hc_autotune(hc_ctx *ctx, hc_tuning *best)
     hc_tuning win = keep;
     win.ms = 1e300;
     for (hc_tuning &t : cand) {
-        HC_TRY(hc_set_tuning(ctx, &t));
         double ms = 1e300;
-        for (int rep = 0; rep < 3; rep++) {
-            HC_TRY(run_evaluation(c, 0, 0.0, 0, false));
+        int r = hc_set_tuning(ctx, &t);
+        for (int rep = 0; rep < 3 && r == HC_OK; rep++) {
+            r = run_evaluation(c, 0, 0.0, 0, false);
             ms = std::min(ms, (double)c->build_ms + (double)c->walk_ms);
+        }
+        if (r != HC_OK) {                  // keep the caller's tuning and the error message
+            const std::string err = c->err;
+            hc_set_tuning(ctx, &keep);
+            c->err = err;
+            return r;
         }
         t.ms = ms;
         if (ms < win.ms) win = t;
