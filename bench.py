@@ -676,9 +676,10 @@ def run_reference(args, world, rank):
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
-    sample = (f"oracle port of hackcode1's maketree/hackgrav (the reference's C cannot be built on this host: "
-              f"its sources are absent here), {procs} processes: each builds the full {n}-body tree and walks "
-              f"{args.ref_sample} sampled bodies; throughput = N / (build + N / (procs x walk rate))")
+    sample = (f"oracle port of hackcode1's maketree/hackgrav in C (bit-identical to the reference's load.c and "
+              f"grav.c where those compile; the GPU host has no NEMO sources), {procs} processes: each builds "
+              f"the full {n}-body tree and walks {args.ref_sample} sampled bodies; "
+              f"throughput = N / (build + N / (procs x walk rate))")
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / value * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic: Plummer (ran3, seed=1)",
