@@ -217,11 +217,9 @@ int hc_mlp_infer_impl(hc_ctx *c, const float *x_dev, int64_t n, float *logits_de
 int hc_mlp_grad_impl(hc_ctx *c, const float *x, const float *y, const float *w, int64_t n, float inv_norm,
                      float *grad_dev, float *loss_dev)
 {
-    static bool attr = false;
-    if (!attr) {
-        HC_CUDA(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)grad_smem()));
-        attr = true;
-    }
+    // per call: the attribute belongs to the current device, and a process may
+    // drive contexts on several
+    HC_CUDA(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)grad_smem()));
     const int nblk = (int)((n + TB - 1) / TB);
     if (nblk > c->mlp_gcap) return HC_ERR_ARG;
     k_mlp_grad<<<nblk, GT, grad_smem(), c->stream>>>(c->mlp_p, x, y, w, n, inv_norm, c->mlp_gpart, c->mlp_lpart);
