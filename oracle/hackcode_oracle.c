@@ -677,6 +677,21 @@ static void diagnostics(int n, const double *mass, const double *pos, const doub
     for (k = 0; k < 6; k++) d->cmphase[k] = d->cmphase[k] / d->mtot;
 }
 
+/* Optional record of every major output (PhaseSpace written): per output
+ * 1 + 10 n doubles -- tnow, then phase [n][2][3], phi [n], acc [n][3] as
+ * output() writes them (code_io.c:139-151).  Set before hco_hackcode1. */
+static double *snap_sink = NULL;
+static int snap_max = 0, snap_count = 0;
+
+void hco_set_snapshot_sink(double *buf, int maxsnaps)
+{
+    snap_sink = buf;
+    snap_max = buf ? maxsnaps : 0;
+    snap_count = 0;
+}
+
+int hco_snapshot_count(void) { return snap_count; }
+
 /* Run hackcode1 from given initial data.  phase [n][2][3] is updated in
  * place; acc [n][3] and phi [n] hold the last force evaluation.  Log rows
  * (at most maxrows) and the bsf statistic of out= are returned.  The
@@ -765,6 +780,18 @@ int hco_hackcode1(int n, const double *mass, double *phase, double *acc, double 
             for (k = 0; k < 9; k++) bsf_add(bsf, d.peten[k]);
             for (k = 0; k < 9; k++) bsf_add(bsf, d.amten[k]);
             for (k = 0; k < 6; k++) bsf_add(bsf, d.cmphase[k]);
+        }
+        if ((bits & 2) && snap_sink && snap_count < snap_max) {
+            double *o = snap_sink + (size_t)snap_count * (1 + 10 * (size_t)n);
+            o[0] = tnow;
+            for (i = 0; i < n; i++)
+                for (k = 0; k < 3; k++) {
+                    o[1 + 6 * i + k] = pos[3 * i + k];
+                    o[1 + 6 * i + 3 + k] = vel[3 * i + k];
+                }
+            memcpy(o + 1 + 6 * (size_t)n, phi, sizeof(double) * (size_t)n);
+            memcpy(o + 1 + 7 * (size_t)n, acc, sizeof(double) * 3 * (size_t)n);
+            snap_count++;
         }
         /* kick-drift-kick remainder: code.c:182-188 */
         for (i = 0; i < n; i++)

@@ -16,25 +16,38 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+import time
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFDIR_DEFAULT = "/root/reference"
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 
 
+def reference_sources() -> str | None:
+    """Directory holding the NEMO sources of the `ref` build: the staged copy
+    in baseline/_ref/nemo (staged first from the NEMO tree where there is
+    one), else None."""
+    from oracle import stage_reference as S
+    return S.stage() if S.source_dir() else S.staged()
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile the oracle (and the reference libs when the sources exist)."""
+    """Compile the oracle, and the reference libs (oracle/_ref) when the
+    reference sources are present (ref=None) or required (ref=True)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    refdir = os.environ.get("NEMO_REFDIR", REFDIR_DEFAULT)
-    if ref is None:
-        ref = os.path.isdir(os.path.join(refdir, "src/nbody/evolve/hackcode/hackcode1"))
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True)
+    if ref is False:
+        return
+    refdir = reference_sources()
+    if refdir is None:
+        if ref:
+            raise FileNotFoundError("no reference sources: set NEMO_REFDIR or stage baseline/_ref/nemo")
+        print("oracle: reference sources absent, oracle/_ref not built")
+        return
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True)
 
 
 class Params(C.Structure):
@@ -96,6 +109,7 @@ def lib():
                                     C.POINTER(C.c_double)]
         L.hco_hackcode1.restype = C.c_int
         L.hco_diagnostics.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp]
+        L.hco_set_snapshot_sink.argtypes = [C.c_void_p, C.c_int]
         assert L.hco_sizeof_logrow() == C.sizeof(LogRow)
         assert L.hco_sizeof_params() == C.sizeof(Params)
         assert L.hco_sizeof_bsf() == C.sizeof(Bsf)
@@ -170,9 +184,14 @@ class Tree:
                               d["quad"], d["body_parent_level"])
         return d
 
-    def forces(self, tol, eps, usequad=False, test_pos=None, skip_self=True):
-        """hackgrav at every body (self skipped) or at test_pos (nothing skipped)."""
-        if test_pos is None:
+    def forces(self, tol, eps, usequad=False, test_pos=None, skip_self=True, idx=None):
+        """hackgrav at every body (self skipped), at the bodies idx (each
+        skipping itself) or at test_pos (nothing skipped)."""
+        if idx is not None:
+            idx = np.ascontiguousarray(idx, dtype=np.int32)
+            tp = np.ascontiguousarray(self._pos[idx])
+            skip = idx
+        elif test_pos is None:
             tp = self._pos
             skip = np.arange(len(tp), dtype=np.int32) if skip_self else None
         else:
@@ -210,10 +229,12 @@ def direct(mass, pos, test_pos=None, eps=0.05, skip=None):
 
 def hackcode1(mass, phase, tnow=0.0, freq=32.0, eps=0.05, tol=1.0, fcells=1.0, tstop=2.0,
               freqout=4.0, minor_freqout=32.0, options="mass,phase", usequad=False,
-              write_out=True, maxrows=100000):
+              write_out=True, maxrows=100000, snapshots=None):
     """Run the hackcode1 integration loop (code.c:57-64,159-191) on the CPU.
 
-    Returns (phase, acc, phi, rows, bsf, (rmin, rsize))."""
+    Returns (phase, acc, phi, rows, bsf, (rmin, rsize)).  When `snapshots` is
+    a list, each major output (tnow, phase[n,2,3], phi[n], acc[n,3]) is
+    appended to it."""
     opts = [w.strip() for w in options.split(",")]
     prm = Params(freq, eps, tol, fcells, tstop, freqout, minor_freqout, int(usequad),
                  int("mass" in opts), int("phi" in opts), int("acc" in opts), int(write_out))
@@ -226,8 +247,21 @@ def hackcode1(mass, phase, tnow=0.0, freq=32.0, eps=0.05, tol=1.0, fcells=1.0, t
     bsf = Bsf()
     rmin = np.zeros(3)
     rsize = C.c_double()
-    nr = lib().hco_hackcode1(n, mass, ph, acc, phi, float(tnow), C.byref(prm), rows, maxrows,
-                             C.byref(bsf), rmin, C.byref(rsize))
+    sink = None
+    if snapshots is not None:
+        nmax = int((tstop - tnow) * freqout + 3) if freqout > 0 else 0
+        sink = np.zeros((max(nmax, 1), 1 + 10 * n))
+        lib().hco_set_snapshot_sink(sink.ctypes.data_as(C.c_void_p), len(sink))
+    try:
+        nr = lib().hco_hackcode1(n, mass, ph, acc, phi, float(tnow), C.byref(prm), rows, maxrows,
+                                 C.byref(bsf), rmin, C.byref(rsize))
+        if sink is not None:
+            for o in sink[:lib().hco_snapshot_count()]:
+                snapshots.append((float(o[0]), o[1:1 + 6 * n].reshape(n, 2, 3).copy(),
+                                  o[1 + 6 * n:1 + 7 * n].copy(), o[1 + 7 * n:].reshape(n, 3).copy()))
+    finally:
+        if sink is not None:
+            lib().hco_set_snapshot_sink(None, 0)
     if nr < 0:
         raise RuntimeError(f"oracle hackcode1 failed: status {nr}")
     return ph, acc, phi, list(rows[:min(nr, maxrows)]), bsf, (rmin, rsize.value)
@@ -250,8 +284,12 @@ class Reference:
 
     _inst: dict = {}
 
-    def __init__(self, quad: bool, max_nbody: int, fcells: float = 1.0):
+    def __init__(self, quad: bool, max_nbody: int, fcells: float = 1.0, nemo_flags: bool = False):
         name = "libhcref_qp.so" if quad else "libhcref_mp.so"
+        if nemo_flags:                   # the build with NEMO's own compiler flags
+            if not quad:
+                raise ValueError("the NEMO-flags build is the quadrupole variant")
+            name = "libhcref_qp_nemo.so"
         path = os.path.join(HERE, "_ref", name)
         if not os.path.exists(path):
             raise FileNotFoundError(path)
@@ -260,6 +298,7 @@ class Reference:
         L.ref_maketree.argtypes = [C.c_int, _dp, _dp, _dp, C.POINTER(C.c_double)]
         L.ref_tree_dump.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _ip]
         L.ref_forces.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, _dp, _dp, _lp, _lp]
+        L.ref_forces_idx.argtypes = [C.c_int, _ip, C.c_double, C.c_double, _dp, _dp, _lp, _lp]
         L.ref_ran3_sequence.argtypes = [C.c_int, C.c_int, _dp]
         L.ref_error_message.restype = C.c_char_p
         L.ref_init(max_nbody, fcells)
@@ -268,18 +307,19 @@ class Reference:
         self.quad = quad
 
     @classmethod
-    def get(cls, quad: bool, max_nbody: int = 1 << 18):
-        key = bool(quad)
+    def get(cls, quad: bool, max_nbody: int = 1 << 18, nemo_flags: bool = False):
+        key = (bool(quad), bool(nemo_flags))
         inst = cls._inst.get(key)
         if inst is None:
-            inst = cls._inst[key] = cls(quad, max_nbody)
+            inst = cls._inst[key] = cls(quad, max_nbody, nemo_flags=nemo_flags)
         if inst.max_nbody < max_nbody:
             raise RuntimeError("reference cell pool was sized for fewer bodies")
         return inst
 
     @staticmethod
-    def available() -> bool:
-        return os.path.exists(os.path.join(HERE, "_ref", "libhcref_qp.so"))
+    def available(nemo_flags: bool = False) -> bool:
+        name = "libhcref_qp_nemo.so" if nemo_flags else "libhcref_qp.so"
+        return os.path.exists(os.path.join(HERE, "_ref", name))
 
     def build(self, mass, pos, rmin=(-2.0, -2.0, -2.0), rsize=4.0):
         self._mass = np.ascontiguousarray(mass, dtype=np.float64)
@@ -315,7 +355,76 @@ class Reference:
         self._L.ref_forces(n, nt, tp, float(tol), float(eps), acc, phi, n2b, nbc)
         return acc, phi, n2b, nbc
 
+    def forces_idx(self, tol, eps, idx):
+        """hackgrav at the loaded bodies idx only, each skipping itself."""
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        nt = len(idx)
+        acc = np.zeros((nt, 3))
+        phi = np.zeros(nt)
+        n2b = np.zeros(nt, np.int64)
+        nbc = np.zeros(nt, np.int64)
+        self._L.ref_forces_idx(nt, idx, float(tol), float(eps), acc, phi, n2b, nbc)
+        return acc, phi, n2b, nbc
+
     def ran3_sequence(self, seed: int, count: int) -> np.ndarray:
         out = np.zeros(count)
         self._L.ref_ran3_sequence(seed, count, out)
         return out
+
+
+# ---------------------------------------------------------------- falcON (gyrfalcON's solver)
+
+class Falcon:
+    """falcON's force solver, the engine of gyrfalcON (usr/dehnen/falcON,
+    Dehnen 2000, 2002), through its C interface (inc/forces_C.h): compiled
+    from the NEMO sources by `oracle/Makefile falcon` into _ref/libfalcon.so
+    (single precision, as falcON builds by default).  One process-wide
+    instance: the C interface keeps one tree."""
+
+    _inst = None
+
+    def __init__(self):
+        path = os.path.join(HERE, "_ref", "libfalcon.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = C.CDLL(path)
+        fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.falcON_initialize.argtypes = [_ip, fp, fp, C.c_void_p, fp, fp, C.c_void_p, C.c_int, C.c_int,
+                                        C.c_float, C.c_float, C.c_int, C.c_float]
+        L.falcON_grow.argtypes = [C.c_int]
+        L.falcON_default_Ncrit.restype = C.c_int
+        L.falcON_default_theta.restype = C.c_float
+        self._L = L
+        self._keep = None
+
+    @classmethod
+    def get(cls):
+        if cls._inst is None:
+            cls._inst = cls()
+        return cls._inst
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(os.path.join(HERE, "_ref", "libfalcon.so"))
+
+    def forces(self, mass, pos, eps, theta, kernel=0, G=1.0, ncrit=None):
+        """One force evaluation of every body: falcON_grow (tree) then
+        falcON_approx_grav (gravity).  theta > 0: falcON's mass-dependent
+        opening angle with minimum theta (gyrfalcON's default mode); theta < 0:
+        fixed -theta.  Returns (acc[n,3], pot[n], grow s, approx_grav s)."""
+        n = len(mass)
+        flags = np.ones(n, np.int32)                 # bit 1: active (wants forces)
+        m = np.ascontiguousarray(mass, dtype=np.float32)
+        x = np.ascontiguousarray(pos, dtype=np.float32).reshape(n, 3)
+        acc = np.zeros((n, 3), np.float32)
+        pot = np.zeros(n, np.float32)
+        self._keep = (flags, m, x, acc, pot)         # the library holds these pointers
+        L = self._L
+        L.falcON_initialize(flags, m, x, None, acc, pot, None, n, 0, float(eps), float(theta), int(kernel),
+                            float(G))
+        t0 = time.perf_counter()
+        L.falcON_grow(int(ncrit) if ncrit else L.falcON_default_Ncrit())
+        t1 = time.perf_counter()
+        L.falcON_approx_grav()
+        t2 = time.perf_counter()
+        return acc.astype(np.float64), pot.astype(np.float64), t1 - t0, t2 - t1

@@ -196,6 +196,26 @@ int ref_forces(int n, int ntest, const double *tpos, double tol_, double eps_,
     return ntest;
 }
 
+/* hackgrav (grav.c:22-32) at the loaded bodies idx[0..nidx) only, each
+ * skipping itself as hackcode1's force loop does (code.c:170-174): a sample
+ * of a large system, or one worker's share of it. */
+int ref_forces_idx(int nidx, const int *idx, double tol_, double eps_,
+                   double *acc, double *phi, int64_t *n2b, int64_t *nbc)
+{
+    int i, k;
+    tol = tol_;
+    eps = eps_;
+    for (i = 0; i < nidx; i++) {
+        bodyptr p = &btab[idx[i]];
+        hackgrav(p);
+        phi[i] = Phi(p);
+        for (k = 0; k < NDIM; k++) acc[3 * i + k] = Acc(p)[k];
+        if (n2b) n2b[i] = n2bterm;
+        if (nbc) nbc[i] = nbcterm;
+    }
+    return nidx;
+}
+
 /* ran3 as linked from the reference (ran3.c:43-94): fill out[] with the
  * first count deviates after seeding with -seed, as set_xrandom does. */
 extern real ran3(int *);

@@ -238,21 +238,52 @@ def test_direct_sample_and_force_error(hc, oracle_lib):
 
 
 def test_hackcode1_run_energy_and_log(hc, oracle_lib):
-    """Config-1 shape (N=4096 Plummer, tol=0.7, eps=0.05, dt=1/32) for 16
-    steps: log counts identical to the oracle each step; energy drift within
-    10% of the oracle's (plus a floor of 1e-6 of |E|)."""
+    """The first configuration in full: mkplummer N=4096 seed=123, tol=0.7,
+    eps=0.05, freq=32, tstop=2 (64 steps, 65 force evaluations),
+    freqout=minor_freqout=2, options=mass,phi,acc (code.c:57-64,159-191;
+    code_io.c:111-154).  Against the oracle's run of the same keywords:
+      * a log row every step with the same interaction counts (nttot, nbavg,
+        ncavg);
+      * energy drift within 10% of the oracle's (plus 1e-6 |E|);
+      * the snapshots at t = 0, 0.5, 1, 1.5, 2: the first force evaluation's
+        acc/phi within 1e-5 relative on >= 99.9% of bodies, the later
+        phase-space states close (FP32 forces change the last bits each step;
+        the tolerances below hold that drift)."""
     O = oracle_lib
     m, ph = O.mkplummer(4096, 123)
-    kw = dict(freq=32.0, eps=0.05, tol=0.7, tstop=0.5, freqout=2.0, minor_freqout=2.0)
-    _, _, _, rows, _, box = O.hackcode1(m, ph, write_out=False, **kw)
-    res = hc.hackcode1(m, ph, options="mass,phi,acc", keep_snapshots=False, **kw)
-    assert len(res.rows) == len(rows)
+    kw = dict(freq=32.0, eps=0.05, tol=0.7, tstop=2.0, freqout=2.0, minor_freqout=2.0)
+    osnaps = []
+    _, _, _, rows, _, box = O.hackcode1(m, ph, write_out=False, options="mass,phi,acc", snapshots=osnaps, **kw)
+    res = hc.hackcode1(m, ph, options="mass,phi,acc", keep_snapshots=True, **kw)
+    assert len(res.rows) == len(rows) == 65
     for rg, ro in zip(res.rows, rows):
-        assert rg.nttot == ro.nttot and rg.nbavg == ro.nbavg and rg.ncavg == ro.ncavg
+        assert rg.nttot == ro.nttot and rg.nbavg == ro.nbavg and rg.ncavg == ro.ncavg, ro.tnow
     e0, e1 = rows[0].etot[0], rows[-1].etot[0]
     g0, g1 = res.rows[0].etot[0], res.rows[-1].etot[0]
+    print(f"energy drift: gpu {g1 - g0:.4e} oracle {e1 - e0:.4e}")
     assert abs((g1 - g0) - (e1 - e0)) <= 0.1 * abs(e1 - e0) + 1e-6 * abs(e0)
     assert np.array_equal(res.box[0], box[0]) and res.box[1] == box[1]
+    gsnaps = [s for s in res.snapshots if s[1] & 2]
+    assert [s[0] for s in gsnaps] == [s[0] for s in osnaps] == [0.0, 0.5, 1.0, 1.5, 2.0]
+    for k, (gs, os_) in enumerate(zip(gsnaps, osnaps)):
+        _, _, gm, gph, gphi, gacc, _ = gs
+        _, oph, ophi, oacc = os_
+        assert np.array_equal(gm, m)
+        dx = np.linalg.norm(gph[:, 0] - oph[:, 0], axis=1) / np.linalg.norm(oph[:, 0], axis=1)
+        dv = np.linalg.norm(gph[:, 1] - oph[:, 1], axis=1) / np.linalg.norm(oph[:, 1], axis=1)
+        ea = _rel_err(gacc, oacc)
+        ep = _rel_err(gphi, ophi)
+        print(f"t={gs[0]}: pos rel diff median {np.median(dx):.2e} max {dx.max():.2e}; vel median "
+              f"{np.median(dv):.2e} max {dv.max():.2e}; acc p99.9 {np.percentile(ea, 99.9):.2e}; "
+              f"phi p99.9 {np.percentile(ep, 99.9):.2e}")
+        if k == 0:
+            assert np.array_equal(gph, oph)
+            assert ((ea <= REL_TOL) & (ep <= REL_TOL)).mean() >= FRACTION
+        else:
+            # measured at t = 2: median 3.5e-8 / max 8.7e-7 (positions), 4.9e-8 / 1.1e-6 (velocities)
+            assert np.median(dx) <= 1e-6 and dx.max() <= 1e-5
+            assert np.median(dv) <= 1e-6 and dv.max() <= 1e-5
+            assert np.percentile(ea, 99.9) <= 1e-5 and np.percentile(ep, 99.9) <= 1e-5
 
 
 def test_hackcode1_testfile_fingerprint(hc, oracle_lib):

@@ -155,3 +155,37 @@ def test_oracle_errors(oracle_lib):
     pos2[3] = pos2[7]                    # coincident -> assert(l != 0)
     T2 = O.Tree(256, 1.0)
     assert T2.build(m, pos2) == 2
+
+
+def test_oracle_at_1m_against_reference_fixture(oracle_lib):
+    """Plummer N=1,048,576 (mkplummer seed=1), tol=0.5, eps=0.01, quadrupoles:
+    the oracle's tree (digest of the canonical cell set and quadrupoles) and
+    the forces and counts of the fixture's 16,384 sampled bodies are the
+    reference's bit for bit (tests/golden/make_golden_plummer1m.py)."""
+    import hashlib
+    O = oracle_lib
+    g = np.load(os.path.join(HERE, "golden", "plummer1m_s1_qp.npz"))
+
+    def digest(*arrays):
+        h = hashlib.sha256()
+        for a in arrays:
+            h.update(np.ascontiguousarray(a).tobytes())
+        return h.hexdigest()
+
+    n = int(g["n"])
+    m, ph = O.mkplummer(n, int(g["seed"]))
+    pos = ph[:, 0].copy()
+    assert digest(m, pos) == str(g["input_digest"])
+    T = O.Tree(n, 1.0)
+    assert T.build(m, pos, True) == 0
+    r, s = T.box()
+    assert np.array_equal(r, g["rmin"]) and s == float(g["rsize"])
+    d = T.dump()
+    c = _canon(d)
+    assert digest(c["level"], c["corner"], c["count"], c["mass"], c["cm"]) == str(g["tree_digest"])
+    assert digest(c["quad"]) == str(g["quad_digest"])
+    assert digest(d["body_parent_level"].astype(np.int32)) == str(g["parent_digest"])
+    idx = g["sample_idx"][::8]                      # 2,048 of the sampled bodies: a few seconds
+    acc, phi, n2b, nbc = T.forces(float(g["tol"]), float(g["eps"]), True, idx=idx)
+    assert np.array_equal(acc, g["sample_acc"][::8]) and np.array_equal(phi, g["sample_phi"][::8])
+    assert np.array_equal(n2b, g["sample_n2b"][::8]) and np.array_equal(nbc, g["sample_nbc"][::8])
