@@ -164,46 +164,119 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# ---------------------------------------------------------------- CPU (oracle) legs
+# ---------------------------------------------------------------- CPU legs (reference code)
 
-def _cpu_worker(args):
-    path, n, nsample, seed, eps = args
-    from oracle import oracle as O
-    d = np.load(path)
-    m, pos = d["mass"], d["pos"]
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_model() -> str:
+    try:
+        for line in open("/proc/cpuinfo"):
+            k, _, v = line.partition(":")
+            if k.strip() in ("model name", "Model"):
+                return v.strip()
+        import platform
+        return platform.processor() or platform.machine()
+    except OSError:
+        return "unknown"
+
+
+class RefWalker:
+    """The CPU implementation of the path that the baselines time: the
+    reference's own load.c / grav.c (oracle/_ref, compiled from the NEMO
+    sources with NEMO's compiler flags) when those sources are present, else
+    the oracle's restatement of them (bit-identical where both exist)."""
+
+    def __init__(self, n: int):
+        from oracle import oracle as O
+        try:
+            O.build(ref=None)
+        except Exception as e:             # a failed ref build leaves the port
+            print(f"bench.py: reference build failed ({e}); timing the oracle port", file=sys.stderr)
+        self.kind = "reference" if O.Reference.available(nemo_flags=True) else "port"
+        if self.kind == "reference":
+            self.R = O.Reference.get(True, n, nemo_flags=True)
+            self.what = ("the reference's own hackcode1 load.c/grav.c (-DQUADPOLE, built from the NEMO sources "
+                         "with NEMO's flags -g -O2)")
+        else:
+            self.T = O.Tree(n, 1.0)
+            self.what = "the oracle's C restatement of hackcode1's load.c/grav.c (NEMO sources absent)"
+
+    def build(self, m, pos):
+        if self.kind == "reference":
+            self.R.build(m, pos)
+        else:
+            self.T.set_box([-2.0, -2.0, -2.0], 4.0)
+            assert self.T.build(m, pos, USEQUAD) == 0
+
+    def walk(self, idx, eps):
+        """Counts (n2b, nbc) of hackgrav at bodies idx, each skipping itself."""
+        if self.kind == "reference":
+            _, _, b, c = self.R.forces_idx(TOL, eps, idx)
+        else:
+            _, _, b, c = self.T.forces(TOL, eps, USEQUAD, idx=idx)
+        return b, c
+
+
+def full_evaluation(w: RefWalker, m, pos, eps, procs: int):
+    """One complete force evaluation on `procs` host cores, as hackforce does
+    it (hackforce.c:177-215): maketree + hackcofm once (serial, as in the
+    reference), then hackgrav for every body, the bodies split into `procs`
+    contiguous shares walked by forked worker processes that share the tree.
+    Returns (seconds, n2b total, nbc total)."""
+    n = len(m)
     t0 = time.perf_counter()
-    T = O.Tree(n, 1.0)
-    T.set_box([-2.0, -2.0, -2.0], 4.0)
-    assert T.build(m, pos, USEQUAD) == 0
+    w.build(m, pos)
+    edges = np.linspace(0, n, procs + 1).astype(np.int64)
+    kids = []
+    for k in range(procs):
+        r, wfd = os.pipe()
+        pid = os.fork()
+        if pid == 0:                       # worker: walk its share, report the totals
+            os.close(r)
+            try:
+                b, c = w.walk(np.arange(edges[k], edges[k + 1], dtype=np.int32), eps)
+                os.write(wfd, np.array([b.sum(), c.sum()], dtype=np.int64).tobytes())
+            finally:
+                os._exit(0)
+        os.close(wfd)
+        kids.append((pid, r))
+    n2b = nbc = 0
+    for pid, r in kids:
+        buf = b""
+        while len(buf) < 16:
+            chunk = os.read(r, 16 - len(buf))
+            if not chunk:
+                break
+            buf += chunk
+        os.close(r)
+        os.waitpid(pid, 0)
+        if len(buf) != 16:
+            raise RuntimeError("bench.py: a reference worker failed")
+        b, c = np.frombuffer(buf, dtype=np.int64)
+        n2b += int(b)
+        nbc += int(c)
+    return time.perf_counter() - t0, n2b, nbc
+
+
+def cpu_baseline_one_core(n, m, pos, eps, nsample, seed=0):
+    """The reference walk on one core: full tree build plus the walks of
+    `nsample` uniformly sampled bodies, extrapolated to one full evaluation.
+    Returns (bodies/s, build seconds, walk bodies/s, kind, what)."""
+    w = RefWalker(n)
+    t0 = time.perf_counter()
+    w.build(m, pos)
     t1 = time.perf_counter()
     rng = np.random.default_rng(seed)
-    idx = rng.choice(n, size=nsample, replace=False)
-    T.forces(TOL, eps, USEQUAD, test_pos=pos[idx])     # test points: same walk, self not skipped
+    idx = np.sort(rng.choice(n, size=min(nsample, n), replace=False)).astype(np.int32)
+    w.walk(idx, eps)
     t2 = time.perf_counter()
-    return t1 - t0, t2 - t1, nsample
-
-
-def cpu_leg(n: int, m, pos, procs: int, nsample_per_proc: int, seed: int = 0, eps: float = EPS):
-    """Oracle port timed on host cores: every process builds the full tree
-    (the reference's build is serial) and walks its own sample of bodies.
-    Returns (bodies/s extrapolated to one full evaluation on `procs` cores,
-    build seconds, walk bodies/s per core)."""
-    import multiprocessing as mp
-    from oracle import oracle as O
-    O.build(ref=False)
-    fd, path = tempfile.mkstemp(suffix=".npz")
-    os.close(fd)
-    np.savez(path, mass=m, pos=pos)
-    try:
-        ctxp = mp.get_context("spawn")
-        with ctxp.Pool(procs) as pool:
-            res = pool.map(_cpu_worker, [(path, n, nsample_per_proc, seed + i, eps) for i in range(procs)])
-    finally:
-        os.remove(path)
-    t_build = statistics.mean(r[0] for r in res)
-    rate = statistics.mean(r[2] / r[1] for r in res)          # bodies/s per core
-    full = t_build + n / (procs * rate)
-    return n / full, t_build, rate
+    rate = len(idx) / (t2 - t1)
+    return n / ((t1 - t0) + n / rate), t1 - t0, rate, w.kind, w.what
 
 
 # ---------------------------------------------------------------- GPU leg
@@ -479,11 +552,11 @@ def run_ours(args, world, rank, local):
     }
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         pos = np.ascontiguousarray(ph[:, 0])
-        v, tb, rate = cpu_leg(n, m, pos, procs=1, nsample_per_proc=args.cpu_sample, eps=eps)
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                               "sample": f"oracle port (C, FP64) of the fixed-theta walk: full tree build of {n} "
-                                         f"bodies ({tb:.2f} s) + walks of {args.cpu_sample} sampled bodies "
-                                         f"({rate:.0f} bodies/s), extrapolated to one full evaluation"}
+        v, tb, rate, kind, what = cpu_baseline_one_core(n, m, pos, eps, args.cpu_sample)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+                               "sample": f"{what}, fixed theta {TOL}, one core ({cpu_model()}): full tree build of "
+                                         f"{n} bodies ({tb:.2f} s) + walks of {args.cpu_sample} uniformly sampled "
+                                         f"bodies ({rate:.0f} bodies/s), extrapolated to one full evaluation"}
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -662,30 +735,39 @@ def run_galaxy(args, world, rank, local):
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, world, rank):
+    """The reference's own CPU implementation of the path on the host cores:
+    every step is one complete force evaluation of the headline workload
+    (maketree + hackcofm, then hackgrav of every body; fixed theta 0.5,
+    eps 0.01, quadrupoles), the walks split over all host cores."""
     if rank != 0:
         return
     from oracle import oracle as O
-    O.build(ref=False)
     n = args.n if args.n else N_DEFAULT
     m, ph = O.mkplummer(n, SEED)
     pos = np.ascontiguousarray(ph[:, 0])
-    procs = os.cpu_count() or 1
-    vals = []
+    procs = host_cores()
+    w = RefWalker(n)
+    secs, totals = [], None
+    wall0 = time.perf_counter()
     for i in range(args.warmup + args.steps):
-        v, tb, rate = cpu_leg(n, m, pos, procs=procs, nsample_per_proc=args.ref_sample, seed=100 * i)
+        t, n2b, nbc = full_evaluation(w, m, pos, EPS, procs)
         if i >= args.warmup:
-            vals.append(v)
-    value = statistics.mean(vals)
-    sample = (f"oracle port of hackcode1's maketree/hackgrav in C (bit-identical to the reference's load.c and "
-              f"grav.c where those compile; the GPU host has no NEMO sources), {procs} processes: each builds "
-              f"the full {n}-body tree and walks {args.ref_sample} sampled bodies; "
-              f"throughput = N / (build + N / (procs x walk rate))")
+            secs.append(t)
+        totals = (n2b, nbc)
+    wall = time.perf_counter() - wall0
+    mean_s = statistics.mean(secs)
+    value = n / mean_s
+    sample = (f"{w.what}; each step one complete evaluation of all {n} bodies: serial tree build, then "
+              f"hackgrav of every body split over {procs} forked processes ({cpu_model()})")
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / value * 1e3, "higher_is_better": True,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic: Plummer (ran3, seed=1)",
-           "config": workload_config(n),
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
-           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": dict(workload_config(n), l2="not applicable (host cores)",
+                          parallelism=f"{procs} host processes (walk split by bodies)"),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": w.kind, "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "interactions": {"n2b": totals[0], "nbc": totals[1]},
+           "wall_s": wall}
     print(json.dumps(out), flush=True)
 
 
@@ -697,8 +779,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=0, help="bodies (default: the workload's)")
     ap.add_argument("--sample", type=int, default=16384, help="bodies for the FP64 force-error sample")
-    ap.add_argument("--cpu-sample", type=int, default=2048)
-    ap.add_argument("--ref-sample", type=int, default=512)
+    ap.add_argument("--cpu-sample", type=int, default=32768,
+                    help="bodies walked by the one-core CPU baseline (about 5-10 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="plummer", choices=["plummer", "hernquist", "ensemble", "galaxy"],
                     help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
