@@ -336,15 +336,19 @@ double hc_nemo_eval(const char *expr, int *ok);
 
 /* Diagnostics sums of device-resident bodies without any device allocation
  * (no counterpart in the reference: an addition for callers that cannot
- * allocate device memory -- e.g. while capturing their own CUDA graph, or
- * inside a runtime that only lends pre-registered buffers).  All pointers are
- * device pointers of n FP64 values; out36 receives the 36 raw sums
- * {KE, PE, KE tensor[9], sum m x_i a_j [9], sum m x_i v_j [9], sum m x[3],
- * sum m v[3], total mass} on `stream` (a cudaStream_t, NULL = default).
- * The per-block partials use a static device array sized for at most
- * 8,388,608 bodies; larger n returns HC_ERR_ARG.  The first call on a device
- * looks the array up (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls on a device share the array: calls that overlap on the
+ * allocate device memory -- a runtime that only lends pre-registered buffers
+ * from its own pool, or a real-time loop that must not pay cudaMalloc's
+ * implicit synchronisation).  All pointers are device pointers of n FP64
+ * values; out36 receives the 36 raw sums {KE, PE, KE tensor[9],
+ * sum m x_i a_j [9], sum m x_i v_j [9], sum m x[3], sum m v[3], total mass}
+ * on `stream` (a cudaStream_t, NULL = default).  PE is 0.5 sum m phi with phi
+ * as passed: with an external field pass phi + phi_ext (hc_diagnostics adds
+ * the external part itself).  The per-block partials use a static device
+ * array sized for at most 8,388,608 bodies; larger n returns HC_ERR_ARG.  The
+ * first call on a device looks the array up (cudaGetSymbolAddress) and should
+ * come before any stream capture; after cudaDeviceReset of a device the
+ * looked-up address is stale and the entry point must not be called on it
+ * again.  All calls on a device share the array: calls that overlap on the
  * GPU race and must be serialised by the caller. */
 int hc_diagnostics_noalloc(int64_t n, const double *mass, const double *x, const double *y, const double *z,
                            const double *vx, const double *vy, const double *vz, const double *ax,

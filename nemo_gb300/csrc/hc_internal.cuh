@@ -239,6 +239,34 @@ int hc_fma_peak_impl(hc_ctx *c, double *tflops);
     } while (0)
 
 #ifdef __CUDACC__
+// Diagnostics sums of one body (code_io.c:160-197) added into acc[36] in the
+// order every diagnostics kernel uses: KE, PE (0.5 m pe_phi), KE tensor[9],
+// m x_i a_j [9], m x_i v_j [9], m x [3], m v [3], m.  Products are rounded
+// separately, as the reference computes them.
+__device__ __forceinline__ void hc_diag_body(double *acc, double m, const double x[3], const double v[3],
+                                             const double a[3], double pe_phi)
+{
+    double velsq = __dmul_rn(v[0], v[0]);
+    velsq = __dadd_rn(velsq, __dmul_rn(v[1], v[1]));
+    velsq = __dadd_rn(velsq, __dmul_rn(v[2], v[2]));
+    const double hm = __dmul_rn(0.5, m);
+    acc[0] += __dmul_rn(hm, velsq);
+    acc[1] += __dmul_rn(hm, pe_phi);
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const double tv = __dmul_rn(v[j], hm), tx = __dmul_rn(x[j], m);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            acc[2 + 3 * j + k] += __dmul_rn(tv, v[k]);
+            acc[11 + 3 * j + k] += __dmul_rn(tx, a[k]);
+            acc[20 + 3 * j + k] += __dmul_rn(tx, v[k]);
+        }
+        acc[29 + j] += tx;
+        acc[32 + j] += __dmul_rn(v[j], m);
+    }
+    acc[35] += m;
+}
+
 // Operands of the packed FP32x2 instructions (__ffma2_rn and relatives): a
 // float2 is one register pair.  Lists stored in pairs keep both entries'
 // values of one quantity adjacent, so lo2 / hi2 of a float4 row give them.

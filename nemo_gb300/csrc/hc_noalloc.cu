@@ -1,15 +1,16 @@
 // hc_noalloc.cu -- diagnostics sums with no device allocation.
 //
 // Some callers of this library cannot allocate device memory at the moment
-// they need the energy / virial / angular-momentum sums: a host program that
-// is in the middle of capturing its own CUDA graph (cudaMalloc is not a
-// capturable operation and would invalidate the capture), a runtime that hands
-// the library only pre-registered buffers from its own memory pool, or a
-// real-time loop that must not pay cudaMalloc's implicit device
-// synchronisation.  hc_diagnostics_noalloc serves them: the caller passes
-// device pointers to the body arrays and to a 36-double result, and the
-// per-block partial sums live in the file-scope array below instead of in
-// memory the library would allocate.
+// they need the energy / virial / angular-momentum sums: a runtime that hands
+// the library only pre-registered buffers from its own memory pool (and
+// accounts for every byte of device memory itself), or a real-time loop that
+// must not pay cudaMalloc's implicit device synchronisation between its
+// steps.  hc_diagnostics_noalloc serves them: the caller passes device
+// pointers to the body arrays and to a 36-double result, and the per-block
+// partial sums live in the file-scope array below instead of in memory the
+// library would allocate.  The potential energy is 0.5 sum m phi with phi as
+// passed: a caller with an external field passes phi + phi_ext, as
+// hc_diagnostics counts it.
 //
 // Limits and sharing:
 //   * the array holds HC_NOALLOC_MAX_BLOCKS partials of 36 doubles (576 KiB);
@@ -22,6 +23,7 @@
 //     serialised by the caller;
 //   * the array keeps the last call's contents, and nothing has to start at
 //     zero: each call reads only the partial slots its own first kernel wrote.
+#include <atomic>
 #include "hc_internal.cuh"
 
 #define HC_NOALLOC_MAX_BLOCKS 2048
@@ -37,8 +39,14 @@ static __device__ __align__(256) double g_partials[HC_NOALLOC_MAX_BLOCKS * NSUM]
 
 // Host side: the device address of g_partials, looked up once per device.
 // (In host code the name g_partials is only a stand-in, not a device address.)
+// Threads whose first calls on a device race all store the same address, so
+// the slots are atomics and no lock is needed.  A failed lookup or launch
+// drops the slot, and the next call looks the address up again.  The address
+// belongs to the device's primary context: after cudaDeviceReset of a device
+// the cached slot is stale, so a process that resets a device must not call
+// this entry point on that device afterwards.
 constexpr int MAX_DEVICES = 64;
-double *g_partials_addr[MAX_DEVICES] = {nullptr};
+std::atomic<double *> g_partials_addr[MAX_DEVICES];
 
 __device__ __forceinline__ double wsum(double v)
 {
@@ -60,27 +68,8 @@ __global__ void __launch_bounds__(THREADS) k_diag_static_part(int64_t n, const d
     const int64_t beg = (int64_t)blockIdx.x * HC_NOALLOC_BODIES_PER_BLOCK;
     const int64_t end = beg + HC_NOALLOC_BODIES_PER_BLOCK < n ? beg + HC_NOALLOC_BODIES_PER_BLOCK : n;
     for (int64_t i = beg + threadIdx.x; i < end; i += THREADS) {
-        const double m = mass[i];
         const double x[3] = {px[i], py[i], pz[i]}, v[3] = {vx[i], vy[i], vz[i]}, a[3] = {ax[i], ay[i], az[i]};
-        double velsq = __dmul_rn(v[0], v[0]);
-        velsq = __dadd_rn(velsq, __dmul_rn(v[1], v[1]));
-        velsq = __dadd_rn(velsq, __dmul_rn(v[2], v[2]));
-        const double hm = __dmul_rn(0.5, m);
-        acc[0] += __dmul_rn(hm, velsq);
-        acc[1] += __dmul_rn(hm, phi[i]);
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            const double tv = __dmul_rn(v[j], hm), tx = __dmul_rn(x[j], m);
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                acc[2 + 3 * j + k] += __dmul_rn(tv, v[k]);
-                acc[11 + 3 * j + k] += __dmul_rn(tx, a[k]);
-                acc[20 + 3 * j + k] += __dmul_rn(tx, v[k]);
-            }
-            acc[29 + j] += tx;
-            acc[32 + j] += __dmul_rn(v[j], m);
-        }
-        acc[35] += m;
+        hc_diag_body(acc, mass[i], x, v, a, phi[i]);     // PE from phi as passed
     }
     __shared__ double sh[THREADS / 32][NSUM];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -118,17 +107,22 @@ extern "C" int hc_diagnostics_noalloc(int64_t n, const double *mass, const doubl
     if (!mass || !x || !y || !z || !vx || !vy || !vz || !ax || !ay || !az || !phi || !out36) return HC_ERR_ARG;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return HC_ERR_CUDA;
-    if (!g_partials_addr[dev]) {
+    double *part = g_partials_addr[dev].load(std::memory_order_acquire);
+    if (!part) {
         // first call on this device: resolve the array's device address with
         // the device current (do this before any stream capture)
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_partials) != cudaSuccess || !p) return HC_ERR_CUDA;
-        g_partials_addr[dev] = (double *)p;
+        part = (double *)p;
+        g_partials_addr[dev].store(part, std::memory_order_release);
     }
-    double *part = g_partials_addr[dev];
     cudaStream_t s = (cudaStream_t)stream;
     const int nblocks = (int)((n + HC_NOALLOC_BODIES_PER_BLOCK - 1) / HC_NOALLOC_BODIES_PER_BLOCK);
     k_diag_static_part<<<nblocks, THREADS, 0, s>>>(n, mass, x, y, z, vx, vy, vz, ax, ay, az, phi, part);
     k_diag_static_final<<<1, 64, 0, s>>>(part, nblocks, out36);
-    return cudaPeekAtLastError() == cudaSuccess ? HC_OK : HC_ERR_CUDA;
+    if (cudaPeekAtLastError() != cudaSuccess) {
+        g_partials_addr[dev].store(nullptr, std::memory_order_release);
+        return HC_ERR_CUDA;
+    }
+    return HC_OK;
 }

@@ -115,29 +115,10 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_part(int64_t n, const dou
 #pragma unroll
     for (int q = 0; q < NDIAG; q++) acc[q] = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double m = mass[i];
         const double x[3] = {px[i], py[i], pz[i]}, v[3] = {vx[i], vy[i], vz[i]}, a[3] = {ax[i], ay[i], az[i]};
-        double velsq = __dmul_rn(v[0], v[0]);
-        velsq = __dadd_rn(velsq, __dmul_rn(v[1], v[1]));
-        velsq = __dadd_rn(velsq, __dmul_rn(v[2], v[2]));
-        const double hm = __dmul_rn(0.5, m);
-        acc[0] += __dmul_rn(hm, velsq);
         // with an external field phi holds tree + external; its energy
         // counts the external part once more (hackcode3/code_io.c:180-186)
-        acc[1] += __dmul_rn(hm, phi_ext ? __dadd_rn(phi[i], phi_ext[i]) : phi[i]);
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            const double tv = __dmul_rn(v[j], hm), tx = __dmul_rn(x[j], m);
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                acc[2 + 3 * j + k] += __dmul_rn(tv, v[k]);
-                acc[11 + 3 * j + k] += __dmul_rn(tx, a[k]);
-                acc[20 + 3 * j + k] += __dmul_rn(tx, v[k]);
-            }
-            acc[29 + j] += tx;
-            acc[32 + j] += __dmul_rn(v[j], m);
-        }
-        acc[35] += m;
+        hc_diag_body(acc, mass[i], x, v, a, phi_ext ? __dadd_rn(phi[i], phi_ext[i]) : phi[i]);
     }
     __shared__ double sh[DIAG_THREADS / 32][NDIAG];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

@@ -1209,7 +1209,15 @@ __global__ void __launch_bounds__(128) k_label(WalkArgs g, const int *gstart, co
                                 rphi[j], rax[j], ray[j], raz[j]);
         } else {
             const int nc = C.y & 255;
-            if (sp + nc > LSTACK) break;          // cannot happen for depth <= 31; stop rather than overflow
+            if (sp + nc > LSTACK) {
+                // cannot happen for depth <= 31; a truncated reference would give a
+                // wrong label, so the label walk reports it instead of passing quietly
+                if (lane == 0) {
+                    atomicCAS(&g.st->error, 0, HC_ERR_STACK);
+                    g.st->info = LSTACK;
+                }
+                break;
+            }
             if (lane < nc) stk[w][sp + lane] = C.x + lane;
             sp += nc;
             __syncwarp();

@@ -617,6 +617,7 @@ Params::Params(const char *const *defv, int argc, char **argv, const char *usage
         vals_[k] = v;
         helps_[k] = help;
     }
+    if (const char *e = getenv("DEBUG")) debug_ = atoi(e);
     std::map<std::string, int> seen;
     bool positional = true;
     size_t posi = 0;
@@ -646,6 +647,7 @@ Params::Params(const char *const *defv, int argc, char **argv, const char *usage
             for (const char *s : SYSTEM_KEYS) sys = sys || k == s;
             if (!sys) fatal(prog_, "Parameter \"" + k + "\" unknown");
             if (k == "help") help_ = true;
+            if (k == "debug") debug_ = atoi(v.c_str());
         }
     }
     if (help_) {

@@ -98,7 +98,11 @@ public:
     const std::string &program() const { return prog_; }
     std::string argv_line() const;
     bool help_requested() const { return help_; }
+    // NEMO's debug level: the debug= system keyword, else $DEBUG, else 0
+    // (src/kernel/io/getparam.c; dprintf(level, ...) prints when debug >= level)
+    int debug_level() const { return debug_; }
 private:
+    int debug_ = 0;
     std::vector<std::string> keys_;
     std::map<std::string, std::string> vals_;
     std::map<std::string, std::string> helps_;

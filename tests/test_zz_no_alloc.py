@@ -1,13 +1,14 @@
 """hc_diagnostics_noalloc: the diagnostics sums without device allocation.
 
-Some callers cannot allocate device memory when they need these sums (for
-example while they are capturing their own CUDA graph, or when a runtime only
-lends them pre-registered buffers).  The entry point takes device pointers to
-the body arrays and to the result and keeps its per-block partials in a static
-device array.  This test calls it through the C ABI twice in a row and checks
-both results against the regular entry point (hc_diagnostics), to the 1e-12
-relative tolerance used for FP64 reductions here.  It lives in a file of its
-own that pytest collects last.
+Some callers cannot allocate device memory when they need these sums (a
+runtime that only lends them pre-registered buffers from its own pool, or a
+real-time loop that must not pay cudaMalloc's implicit synchronisation).  The
+entry point takes device pointers to the body arrays and to the result and
+keeps its per-block partials in a static device array.  This test calls it
+through the C ABI twice in a row and checks both results against the regular
+entry point (hc_diagnostics), to the 1e-12 relative tolerance used for FP64
+reductions here, and checks that the device's free memory is the same before
+and after the calls.  It lives in a file of its own that pytest collects last.
 """
 import ctypes as C
 
@@ -52,12 +53,16 @@ def test_noalloc_diagnostics_match_regular_entry_point():
     out = torch.zeros(36, dtype=torch.float64, device=dev)
     L = hc.library()
     results = []
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()           # cudaMemGetInfo
     for _ in range(2):                                   # two calls in a row share the static array
         out.fill_(np.nan)
         rc = L.hc_diagnostics_noalloc(n, *[t.data_ptr() for t in tens], out.data_ptr(), None)
         assert rc == 0
         torch.cuda.synchronize()
         results.append(out.cpu().numpy().copy())
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)     # nothing was allocated
     for raw in results:
         got = _finish(raw)
         for k, v in ref.items():
