@@ -562,6 +562,94 @@ def run_ours(args, world, rank, local):
         print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------- config-2 leapfrog run
+
+RUN_DT = 1.0 / 128
+
+
+def run_plummer_run(args, world, rank, local):
+    """The second configuration as specified: Plummer N=1,048,576 (mkplummer
+    seed=1), tol=0.5, eps=0.01, quadrupoles; one force evaluation plus
+    `--steps` (default 100) leapfrog steps at dt=1/128 with the FP64 state
+    (stepsystem, code.c:159-191), once with the reference's fixed-theta rule
+    and once with the learned criterion (guard on) at the fixed rule's RMS
+    force error.  Each step is one CUDA-graph replay (build, walk with the
+    closing half-kick, diagnostics) and the kick-drift; FP64 energy and
+    angular-momentum drift and guard trips are reported."""
+    import torch
+    from nemo_gb300 import build as B
+    B.build()
+    from nemo_gb300 import hackcode as hc
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (the CUDA path has no CPU fallback)")
+    torch.cuda.set_device(local)
+    n = args.n if args.n else N_DEFAULT
+    m, ph = hc.mkplummer(n, SEED)
+    ctx = hc.Context(n, tol=TOL, eps=EPS, fcells=1.0, usequad=USEQUAD)
+    ctx.upload(m, ph)
+    ctx.evaluate()
+    TUNING["body"] = ctx.autotune()
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(n, size=min(args.sample, n), replace=False)).astype(np.int64)
+    ea, _ = ctx.direct_sample(idx)
+    fixed = point(ctx, ("body", TOL), idx, ea)
+    err_pt, _ = calibrate(ctx, idx, ea, lambda e: ("error", e), 1e-3, 64.0, fixed["rms"])
+    set_mode(ctx, ("body", TOL))
+    ctx.evaluate()
+    tg = TUNING["group"]
+    ctx.set_tuning(tg["group_max"], tg["list_depth"], tg["grouping"])
+    train = ctx.learn_from_self(theta=err_pt["mode"][1] if err_pt else 0.03, target=1 << 20,
+                                band=tuple(args.train_band))
+    ctx.learn_band(*args.band)
+    lrn_pt, _ = calibrate(ctx, idx, ea, lambda e: ("learned", e, LEARNED_THRESHOLD), 1e-3, 64.0, fixed["rms"])
+    runs = {}
+    with ClockSampler(local) as clk:
+        for name, mode, guard in (("fixed_theta_0.5", ("body", TOL), False),
+                                  ("learned", tuple(lrn_pt["mode"]) if lrn_pt else ("body", TOL), True)):
+            set_mode(ctx, mode)
+            ctx.set_guard(GUARD_SAMPLE if guard else 0, RMS_BUDGET, seed=1)
+            ctx.upload(m, ph)                                   # the run starts from the initial conditions
+            d0, _, _, _ = ctx.step(RUN_DT, 0)                   # the first force evaluation
+            e0, l0 = d0.etot[0], angular_momentum(d0)
+            barrier(world)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(1, args.steps + 1):
+                d, _, _, _ = ctx.step(RUN_DT, k)
+            torch.cuda.synchronize()
+            secs = time.perf_counter() - t0
+            ms = reduce_max(1e3 * secs / args.steps, world)
+            runs[name] = {"mode": list(mode), "ms_per_step": ms, "body_steps_per_s": world * n / (ms * 1e-3),
+                          "energy_drift": abs((d.etot[0] - e0) / e0),
+                          "angular_momentum_drift": float(np.linalg.norm(angular_momentum(d) - l0)
+                                                          / max(np.linalg.norm(l0), 1e-300)),
+                          "interactions_last_step": int(d.n2b + d.nbc)}
+            if guard:
+                runs[name]["guard"] = ctx.guard_stats()
+    ctx.set_guard(0)
+    head = runs["learned"]
+    out = {
+        "metric": "Plummer N=1M leapfrog body-steps/s (config 2: one evaluation + 100 steps at dt=1/128)",
+        "value": head["body_steps_per_s"], "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": 1, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: Plummer sphere drawn as mkplummer does (ran3, seed=1)",
+        "config": {"workload": f"plummer N={n} seed={SEED} (mkplummer), tol={TOL}, eps={EPS}, quadrupole, "
+                               f"dt=1/128, {args.steps} steps after the first evaluation, FP64 leapfrog state",
+                   "timing": "host wall clock over the steps (each step one CUDA-graph replay, synchronised)",
+                   "l2": "working set larger than L2 (no flush)"},
+        "runs": runs,
+        "ratio_learned_vs_fixed_theta": head["body_steps_per_s"] / runs["fixed_theta_0.5"]["body_steps_per_s"],
+        "rms_error": {"fixed_theta_0.5": fixed["rms"], "learned": lrn_pt["rms"] if lrn_pt else None,
+                      "sample": int(len(idx)), "against": "FP64 direct sum (GPU), initial conditions"},
+        "training": train,
+        "clocks": clk.summary(),
+    }
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 # ---------------------------------------------------------------- ensemble workload
 
 ENS_NSYS, ENS_NMIN, ENS_NMAX, ENS_SEED = 4096, 64, 16384, 1
@@ -732,6 +820,89 @@ def run_galaxy(args, world, rank, local):
         print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------- gyrfalcON (falcON) CPU baseline
+
+# falcON opening angles (theta_min of its mass-dependent theta(M), Plummer kernel, eps=0.01) at which
+# its RMS relative force error on this file's 16,384-body sample of the headline system equals the
+# fixed-theta rule's (tol 0.5: 3.62e-4) and 1e-3; found by oracle/calibrate_falcon.py (bisection
+# against an FP64 direct sum): RMS 3.59e-4 and 9.85e-4 there.
+FALCON_THETA = {"equal_rms_fixed_theta_0.5": 0.1587, "rms_1e-3": 0.2457}
+
+
+def _fork_map(fn, items):
+    """Run fn(item) in one forked worker per item; returns the results (pickled through pipes)."""
+    import pickle
+    kids = []
+    for it in items:
+        r, w = os.pipe()
+        pid = os.fork()
+        if pid == 0:
+            os.close(r)
+            try:
+                data = pickle.dumps(fn(it))
+                with os.fdopen(w, "wb") as f:
+                    f.write(data)
+            finally:
+                os._exit(0)
+        os.close(w)
+        kids.append((pid, r))
+    out = []
+    for pid, r in kids:
+        with os.fdopen(r, "rb") as f:
+            data = f.read()
+        os.waitpid(pid, 0)
+        if not data:
+            raise RuntimeError("bench.py: a worker failed")
+        out.append(pickle.loads(data))
+    return out
+
+
+def falcon_leg(m, pos, eps, procs: int, nsample: int = 1024):
+    """gyrfalcON's force solver (falcON, compiled from the NEMO sources) at the
+    calibrated opening angles: one evaluation (tree + gravity of every body)
+    per forked process, `procs` at once; RMS relative force error of one of
+    them on `nsample` sampled bodies against an FP64 direct sum (oracle)."""
+    import subprocess
+    from oracle import oracle as O
+    src = O.reference_sources()
+    if src is None:
+        return {"unavailable": "NEMO sources absent (falcON not staged)"}
+    try:
+        subprocess.run(["make", "-s", f"-j{min(procs, 16)}", "-C", os.path.join(ROOT, "oracle"), "falcon",
+                        f"REFDIR={src}"], check=True, capture_output=True)
+    except subprocess.CalledProcessError as e:
+        return {"unavailable": "falcON build failed: " + (e.stderr or b"").decode()[-300:]}
+    n = len(m)
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(n, size=nsample, replace=False)).astype(np.int64)
+    chunks = np.array_split(idx, procs)
+    parts = _fork_map(lambda ch: O.direct(m, pos, test_pos=pos[ch], eps=eps, skip=ch.astype(np.int32))[0], chunks)
+    ea = np.concatenate(parts)
+    out = {"kernel": 0, "eps": eps, "theta_mode": "theta(M), minimum theta as given (gyrfalcON's default mode)",
+           "cores": procs, "cpu": cpu_model(), "precision": "FP32 (falcON's default build)"}
+    for name, theta in FALCON_THETA.items():
+        if theta is None:
+            continue
+
+        def one(k, theta=theta):
+            acc, _, tg, tv = O.Falcon.get().forces(m, pos, eps, theta, kernel=0)
+            rel = None
+            if k == 0:
+                r = np.linalg.norm(acc[idx] - ea, axis=1) / np.linalg.norm(ea, axis=1)
+                rel = float(np.sqrt(np.mean(r ** 2)))
+            return tg, tv, rel
+
+        t0 = time.perf_counter()
+        res = _fork_map(one, range(procs))
+        wall = time.perf_counter() - t0
+        single = statistics.median(r[0] + r[1] for r in res)
+        out[name] = {"theta": theta, "rms_sampled": res[0][2], "sample": nsample,
+                     "seconds_per_evaluation_one_core": single, "bodies_per_s_one_core": n / single,
+                     "bodies_per_s_all_cores": procs * n / wall,
+                     "all_cores": f"{procs} independent evaluations at once (nemo.bench np= style), wall {wall:.1f} s"}
+    return out
+
+
 # ---------------------------------------------------------------- reference arm
 
 def run_reference(args, world, rank):
@@ -768,13 +939,15 @@ def run_reference(args, world, rank):
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "interactions": {"n2b": totals[0], "nbc": totals[1]},
            "wall_s": wall}
+    if not args.no_falcon:
+        out["gyrfalcON"] = falcon_leg(m, pos, EPS, procs)
     print(json.dumps(out), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 10; plummer-run: 100)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=0, help="bodies (default: the workload's)")
@@ -782,8 +955,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=32768,
                     help="bodies walked by the one-core CPU baseline (about 5-10 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="plummer", choices=["plummer", "hernquist", "ensemble", "galaxy"],
-                    help="plummer: the headline (N=1M); hernquist: N=4M, eps=0.005; "
+    ap.add_argument("--no-falcon", action="store_true", help="reference arm: skip the gyrfalcON (falcON) leg")
+    ap.add_argument("--workload", default="plummer",
+                    choices=["plummer", "plummer-run", "hernquist", "ensemble", "galaxy"],
+                    help="plummer: the headline (N=1M); plummer-run: the same system, one evaluation + "
+                         "100 leapfrog steps; hernquist: N=4M, eps=0.005; "
                          "ensemble: 4096 independent systems; galaxy: 2^24-body disk galaxy, leapfrog")
     ap.add_argument("--nsys", type=int, default=ENS_NSYS)
     ap.add_argument("--train-theta", type=float, default=0.0,
@@ -795,6 +971,8 @@ def main():
     ap.add_argument("--generator", default="host", choices=["host", "device"],
                     help="galaxy workload: draw the bodies with mkgalaxy on the host or hc_generate on the device")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 100 if args.workload == "plummer-run" else 10
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
@@ -802,6 +980,8 @@ def main():
         run_ensemble(args, world, rank, local)
     elif args.workload == "galaxy":
         run_galaxy(args, world, rank, local)
+    elif args.workload == "plummer-run":
+        run_plummer_run(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:
