@@ -187,6 +187,12 @@ int hc_last_timing(hc_ctx *ctx, double *build_ms, double *walk_ms, int64_t *laun
  *     adds an adjacency test a bounding box does not need). */
 enum { HC_CRITERION_BODY = 0, HC_CRITERION_GROUP = 1, HC_CRITERION_ERROR = 2, HC_CRITERION_LEARNED = 3,
        HC_CRITERION_BH86 = 4, HC_CRITERION_SW94 = 5, HC_CRITERION_BARNES = 6 };
+/* The critical radius^2 of every cell of the current tree under one of
+ * treecode1's criteria (HC_CRITERION_BH86/_SW94/_BARNES) at opening angle
+ * theta, as the walk uses them -- setrcrit, treecode1/treeload.c:232-252,
+ * with the cell's geometric centre and size and its centre of mass -- into
+ * rcrit2[ncell], in hc_dump_tree's cell order (FP32 values widened). */
+int hc_tree_rcrit(hc_ctx *ctx, int criterion, double theta, double *rcrit2);
 int hc_set_criterion(hc_ctx *ctx, int criterion, double theta);
 
 /* Guard of the group, error and learned criteria (no counterpart in
@@ -245,8 +251,9 @@ int hc_set_grouping(hc_ctx *ctx, int kind);
 /* External potential added to every body's acceleration and potential after
  * the walk, as hackcode3 does with potname= / potpars= (hackcode3/grav.c:34-38,
  * code.c:136-139): NEMO's plug-ins plummer (par: omega, M, a), hernquist
- * (omega, M, a), miyamoto (omega, M, a, b) and log (omega, m_c, r_c, q, r),
- * restated on the device with the plug-ins' defaults for missing parameters;
+ * (omega, M, a), miyamoto (omega, M, a, b; symmetry axis y, as NEMO builds
+ * miyamoto.c) and log (omega, m_c, r_c, q, r), restated on the device with the
+ * plug-ins' defaults for missing parameters;
  * the pattern speed omega must be 0.  The energy in hc_diag counts the
  * external potential as hackcode3's diagnostics do (code_io.c:180-186).
  * name NULL, "" or "null" turns it off. */

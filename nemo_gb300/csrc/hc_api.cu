@@ -456,6 +456,30 @@ int hc_dump_tree(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count, dou
     return r < 0 ? r : HC_OK;
 }
 
+int hc_tree_rcrit(hc_ctx *c, int criterion, double theta, double *rcrit2)
+{
+    if (!c || !rcrit2 || criterion < HC_CRITERION_BH86 || criterion > HC_CRITERION_BARNES || !(theta >= 0.0))
+        return HC_ERR_ARG;
+    if (!c->have_tree) {
+        c->err = "hc_tree_rcrit: no tree (call hc_build_tree first)";
+        return HC_ERR_STATE;
+    }
+    if (!c->rcrit2) HC_TRY(dalloc(c, &c->rcrit2, c->maxnode));
+    hc_rcrit_launch(c, criterion - HC_CRITERION_BH86 + 1, theta);
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    HC_CUDA(cudaMemcpy(c->h_box, c->box, sizeof(hc_box), cudaMemcpyDeviceToHost));
+    const int nn = c->h_box->nnode;
+    if (nn <= 0) return HC_OK;
+    std::vector<int2> C(nn);
+    std::vector<float> r(nn);
+    HC_CUDA(cudaMemcpy(C.data(), c->nodeC, sizeof(int2) * nn, cudaMemcpyDeviceToHost));
+    HC_CUDA(cudaMemcpy(r.data(), c->rcrit2, sizeof(float) * nn, cudaMemcpyDeviceToHost));
+    int64_t ci = 0;
+    for (int k = 0; k < nn; k++)             // cells in breadth-first order, as hc_dump_tree lists them
+        if (C[k].x >= 0) rcrit2[ci++] = (double)r[k];
+    return HC_OK;
+}
+
 static int forces_self(hc_ctx *c, double kick_dthf, int64_t nstep)
 {
     if (!c->have_tree) {

@@ -35,7 +35,7 @@ __global__ void k_kick_drift(int64_t n, double dt, double *px, double *py, doubl
 
 // External potentials of NEMO's potential plug-ins (pattern speed 0),
 // restated: plummer (M, a) -M/sqrt(r^2 + a^2); hernquist (M, a) -M/(r + a);
-// miyamoto (M, a, b) -M/sqrt(R^2 + (a + sqrt(z^2 + b^2))^2); log (m_c, r_c,
+// miyamoto (M, a, b) -M/sqrt(R^2 + (a + sqrt(y^2 + b^2))^2), R^2 = x^2 + z^2; log (m_c, r_c,
 // q, r) (m_c/r_c) ln(r_c^2 + x^2 + y^2/q^2 + z^2/r^2).
 __device__ __forceinline__ void ext_field(int kind, const double *p, double x, double y, double z, double *ax,
                                           double *ay, double *az, double *pot)
@@ -55,12 +55,15 @@ __device__ __forceinline__ void ext_field(int kind, const double *p, double x, d
         *ay = g * y;
         *az = g * z;
     } else if (kind == HC_EXTPOT_MIYAMOTO) {
-        const double q = sqrt(z * z + p[2] * p[2]), s = sqrt(x * x + y * y + (p[1] + q) * (p[1] + q));
+        // NEMO builds miyamoto.c without -DY/-DZ, which selects its re-oriented
+        // "XZY" setup (miyamoto.c:45-56): the disk's symmetry axis is y
+        const double R = sqrt(x * x + z * z);
+        const double q = sqrt(y * y + p[2] * p[2]), s = sqrt(R * R + (p[1] + q) * (p[1] + q));
         *pot = -p[0] / s;
         const double t = *pot / (s * s);
         *ax = t * x;
-        *ay = t * y;
-        *az = t * z * (p[1] > 0.0 ? (p[1] + q) / q : 1.0);
+        *ay = t * y * (p[1] > 0.0 ? (p[1] + q) / q : 1.0);
+        *az = t * z;
     } else {                                     // HC_EXTPOT_LOG
         const double mor = p[1] > 0.0 ? p[0] / p[1] : p[0];
         const double iq = 1.0 / (p[2] * p[2]), ir = 1.0 / (p[3] * p[3]);

@@ -24,7 +24,8 @@ ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "cell pool exhausted", -4: "
 
 # exported symbols of include/hackcode_gpu.h
 EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_upload", "hc_set_box", "hc_get_box",
-           "hc_build_tree", "hc_tree_summary", "hc_dump_tree", "hc_forces", "hc_forces_at", "hc_download",
+           "hc_build_tree", "hc_tree_summary", "hc_dump_tree", "hc_tree_rcrit", "hc_forces", "hc_forces_at",
+           "hc_download",
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
            "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_mkhernquist", "hc_mkgalaxy", "hc_make_testdata",
            "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate",
@@ -122,6 +123,7 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_build_tree.argtypes = [_vp]
     L.hc_tree_summary.argtypes = [_vp, C.POINTER(TreeInfo)]
     L.hc_dump_tree.argtypes = [_vp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]
+    L.hc_tree_rcrit.argtypes = [_vp, C.c_int, C.c_double, _dp]
     L.hc_forces.argtypes = [_vp]
     L.hc_evaluate.argtypes = [_vp]
     L.hc_set_criterion.argtypes = [_vp, C.c_int, C.c_double]
@@ -312,6 +314,14 @@ class Context:
         self._check(self._L.hc_dump_tree(self._h, d["level"], d["corner"], d["count"], d["mass"], d["cm"],
                                          d["quad"], d["body_parent_level"]))
         return d
+
+    def tree_rcrit(self, criterion: str, theta: float):
+        """Critical radius^2 per cell of treecode1's bh86 / sw94 / barnes ("new") criterion, in
+        dump_tree's cell order."""
+        code = {"bh86": 4, "sw94": 5, "barnes": 6}[criterion]
+        out = np.zeros(int(self.tree_info().ncell))
+        self._check(self._L.hc_tree_rcrit(self._h, code, float(theta), out))
+        return out
 
     def forces(self):
         self._check(self._L.hc_forces(self._h))

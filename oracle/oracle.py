@@ -428,3 +428,113 @@ class Falcon:
         L.falcON_approx_grav()
         t2 = time.perf_counter()
         return acc.astype(np.float64), pot.astype(np.float64), t1 - t0, t2 - t1
+
+
+# ---------------------------------------------------------------- treecode1's setrcrit (reference)
+
+def tc1_available() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libtc1ref.so"))
+
+
+def tc1_setrcrit(criterion: str, theta: float, rsize: float, center, size, cm) -> np.ndarray:
+    """Rcrit2 of cells (geometric centre, side, centre of mass) as treecode1's
+    own setrcrit assigns it (treecode1/treeload.c:232-252, compiled from the
+    NEMO sources into _ref/libtc1ref.so); criterion bh86 / sw94 / barnes."""
+    L = C.CDLL(os.path.join(HERE, "_ref", "libtc1ref.so"))
+    L.ref_setrcrit.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
+    center = np.ascontiguousarray(center, dtype=np.float64).reshape(-1, 3)
+    size = np.ascontiguousarray(size, dtype=np.float64).reshape(-1)
+    cm = np.ascontiguousarray(cm, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(len(size))
+    L.ref_setrcrit({"bh86": 1, "sw94": 2, "barnes": 3}[criterion], float(theta), float(rsize), len(size),
+                   center, size, cm, out)
+    return out
+
+
+# ---------------------------------------------------------------- NEMO potential plug-ins (reference)
+
+def potential_available(name: str) -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", f"libpot_{name}.so"))
+
+
+def ref_potential(name: str, pars, pos):
+    """acc[n,3], pot[n] of NEMO's potential plug-in `name` (plummer, hernquist,
+    miyamoto, log: src/orbit/potential/data/<name>.c compiled from the NEMO
+    sources into _ref/libpot_<name>.so) with potpars `pars` (pattern speed
+    first), at time 0."""
+    # A plug-in keeps parameters that potpars= does not give from its previous
+    # initialisation (file-scope statics); NEMO loads it afresh in each
+    # program, so each call here loads a fresh copy.
+    import shutil
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, f"libpot_{name}.so")
+        shutil.copyfile(os.path.join(HERE, "_ref", f"libpot_{name}.so"), path)
+        L = C.CDLL(path, mode=C.RTLD_LOCAL)
+        L.ref_pot_eval.argtypes = [C.c_int, _dp, C.c_int, _dp, _dp, _dp]
+        par = np.ascontiguousarray(pars if len(pars) else [0.0], dtype=np.float64)
+        x = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        acc = np.zeros_like(x)
+        pot = np.zeros(len(x))
+        L.ref_pot_eval(len(pars), par, len(x), x, acc, pot)
+        del L
+    return acc, pot
+
+
+# ---------------------------------------------------------------- hackcode1 state files (reference)
+
+_STATE_KEYS = ("freq", "tol", "eps", "fcells", "tstop", "freqout", "minor_freqout", "tnow", "tout", "minor_tout",
+               "rsize")
+
+
+def state_available() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libstateref.so"))
+
+
+def _state_lib():
+    L = C.CDLL(os.path.join(HERE, "_ref", "libstateref.so"))
+    L.ref_state_identity.argtypes = [C.c_char_p, C.c_char_p]
+    L.ref_state_write.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, _dp, C.c_int, _dp, C.c_int, _dp, _dp, _dp, _dp]
+    L.ref_state_read.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, _dp, C.POINTER(C.c_int), _dp,
+                                 C.POINTER(C.c_int), _dp, _dp, _dp, _dp]
+    L.ref_state_error.restype = C.c_char_p
+    return L
+
+
+def ref_state_write(path, state: dict, program="hackcode1", version="1.5b"):
+    """Write a state file with hackcode1's own savestate (code_io.c:222-248,
+    NEMO's filestruct writer).  state: the _STATE_KEYS, headline, options,
+    nstep, rmin, mass, phase, acc, phi."""
+    L = _state_lib()
+    L.ref_state_identity(program.encode(), version.encode())
+    dbl = np.array([state[k] for k in _STATE_KEYS] + [0.0])
+    n = len(state["mass"])
+    rc = L.ref_state_write(str(path).encode(), state["headline"].encode(), state["options"].encode(), dbl,
+                           int(state["nstep"]), np.ascontiguousarray(state["rmin"], dtype=np.float64), n,
+                           np.ascontiguousarray(state["mass"], dtype=np.float64),
+                           np.ascontiguousarray(state["phase"], dtype=np.float64),
+                           np.ascontiguousarray(state["acc"], dtype=np.float64),
+                           np.ascontiguousarray(state["phi"], dtype=np.float64))
+    if rc:
+        raise RuntimeError("reference savestate failed: " + L.ref_state_error().decode())
+
+
+def ref_state_read(path, nmax: int = 1 << 20) -> dict:
+    """Read a state file with hackcode1's own restorestate (code_io.c:254-284)."""
+    L = _state_lib()
+    hl = C.create_string_buffer(1024)
+    op = C.create_string_buffer(1024)
+    dbl = np.zeros(12)
+    nstep = C.c_int()
+    rmin = np.zeros(3)
+    n = C.c_int(nmax)
+    mass, phase, acc, phi = np.zeros(nmax), np.zeros((nmax, 2, 3)), np.zeros((nmax, 3)), np.zeros(nmax)
+    rc = L.ref_state_read(str(path).encode(), hl, op, 1024, dbl, C.byref(nstep), rmin, C.byref(n), mass, phase,
+                          acc, phi)
+    if rc:
+        raise RuntimeError(f"reference restorestate failed ({rc}): " + L.ref_state_error().decode())
+    k = n.value
+    out = {key: float(v) for key, v in zip(_STATE_KEYS, dbl)}
+    out.update(headline=hl.value.decode(), options=op.value.decode(), nstep=nstep.value, rmin=rmin,
+               mass=mass[:k], phase=phase[:k], acc=acc[:k], phi=phi[:k])
+    return out

@@ -29,6 +29,15 @@ HC1 = "src/nbody/evolve/hackcode/hackcode1"
 FILES = [
     f"{HC1}/load.c", f"{HC1}/grav.c", f"{HC1}/code.h", f"{HC1}/defs.h", f"{HC1}/proto.h",
     "src/kernel/numrec/ran3.c",
+    "src/nbody/evolve/hackcode/treecode1/treeload.c", "src/nbody/evolve/hackcode/treecode1/treedefs.h",
+    "src/nbody/evolve/hackcode/treecode1/treecode.h",
+    "src/orbit/potential/data/plummer.c", "src/orbit/potential/data/hernquist.c",
+    "src/orbit/potential/data/miyamoto.c", "src/orbit/potential/data/log.c", "inc/potential_float.h",
+    f"{HC1}/code_io.c", "src/kernel/io/filesecret.c", "src/kernel/io/filesecret.h", "src/kernel/io/extstring.c",
+    "src/kernel/io/convert.c", "src/kernel/io/ieeehalfprecision.c", "src/kernel/io/stropen.c",
+    "src/kernel/cores/strlib.c", "src/kernel/cores/bswap.c", "inc/extstring.h", "inc/filestruct.h",
+    "inc/history.h", "inc/strlib.h", "inc/snapshot/snapshot.h", "inc/snapshot/get_snap.c",
+    "inc/snapshot/get_snap-old.c", "inc/snapshot/put_snap.c", "inc/snapshot/put_snap-old.c",
     "inc/stdinc.h", "inc/vectmath.h", "inc/mathfns.h", "inc/getparam.h", "inc/options.h",
 ]
 # falcON's library without NEMO I/O (its makepub's non-NEMO object list, less

@@ -1,8 +1,11 @@
 """GPU tests of the external potential (hackcode3's potname= / potpars=):
-the added field against the plug-ins' formulas, the energy convention of the
-diagnostics, energy conservation of test bodies orbiting in the field
-through graph-replayed leapfrog steps, argument errors, and the drop-in
-program's keywords."""
+the added field against NEMO's own plug-ins (src/orbit/potential/data/
+{plummer,hernquist,miyamoto,log}.c, compiled from the NEMO sources into
+oracle/_ref) where those are staged, else against the plug-ins' formulas
+restated below (the two agree: tests/test_oracle_golden.py); the energy
+convention of the diagnostics, energy conservation of test bodies orbiting
+in the field through graph-replayed leapfrog steps, argument errors, and the
+drop-in program's keywords."""
 import os
 import subprocess
 
@@ -38,11 +41,12 @@ def field(kind, pars, x):
         r = np.linalg.norm(x, axis=1)
         return (-M / (r * (r + a) ** 2))[:, None] * x, -M / (r + a)
     if kind == "miyamoto":
+        # NEMO's default build of miyamoto.c: symmetry axis y (its "XZY setup")
         M, a, b = (p + [1.0, 0.0, 1.0][len(p):])[:3]
-        q = np.sqrt(z0 ** 2 + b * b)
-        s = np.sqrt(x0 ** 2 + y0 ** 2 + (a + q) ** 2)
+        q = np.sqrt(y0 ** 2 + b * b)
+        s = np.sqrt(x0 ** 2 + z0 ** 2 + (a + q) ** 2)
         f = -M / s ** 3
-        return np.stack([f * x0, f * y0, f * z0 * ((a + q) / q if a > 0 else 1.0)], 1), -M / s
+        return np.stack([f * x0, f * y0 * ((a + q) / q if a > 0 else 1.0), f * z0], 1), -M / s
     mc, rc, q = (p + [1.0, 1.0, 1.0][len(p):])[:3]
     r = p[3] if len(p) > 3 else q
     mor = mc / rc if rc > 0 else mc
@@ -56,7 +60,7 @@ CASES = [("plummer", [0.0, 2.0, 1.5]), ("hernquist", [0.0, 3.0, 0.5]), ("miyamot
 
 
 @pytest.mark.parametrize("kind,pars", CASES)
-def test_field_added_after_the_walk(hc, kind, pars):
+def test_field_added_after_the_walk(hc, oracle_lib, kind, pars):
     n = 4096
     m, ph = hc.mkplummer(n, 21)
     ctx = hc.Context(n, tol=0.6, eps=0.02, usequad=True)
@@ -66,7 +70,10 @@ def test_field_added_after_the_walk(hc, kind, pars):
     ctx.set_extpot(kind, pars)
     ctx.evaluate()
     _, a1, p1 = ctx.download(phase=False)
-    ae, pe = field(kind, pars, ph[:, 0])
+    if oracle_lib.potential_available(kind):
+        ae, pe = oracle_lib.ref_potential(kind, pars, ph[:, 0])       # the reference's plug-in
+    else:
+        ae, pe = field(kind, pars, ph[:, 0])
     np.testing.assert_allclose(a1 - a0, ae, rtol=1e-10, atol=1e-12 * np.abs(ae).max())
     np.testing.assert_allclose(p1 - p0, pe, rtol=1e-10, atol=1e-12)
     # energy: hackcode3 counts the external potential once more in U

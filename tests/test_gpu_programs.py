@@ -6,7 +6,8 @@
 * ``hackforce`` must agree with the oracle per body (counts exact, forces to
   1e-5) with and without test=;
 * a run saved with save= and continued with restart= must end in the same
-  state as an uninterrupted run;
+  state as an uninterrupted run, and its state file is the one hackcode1's
+  own savestate writes (read and re-written by the reference's code);
 * the extensions dtime= / nstep= / usequad= drive the same integration as
   freq= / tstop= with the quadrupole build.
 """
@@ -124,6 +125,38 @@ def test_save_and_restart_continue_the_run(progs, tmp_path):
     assert b[-1].time == full[-1].time == 1.0
     assert np.array_equal(b[-1].phase, full[-1].phase)
     assert np.array_equal(b[-1].acc, full[-1].acc)
+
+
+def test_state_file_is_the_references(progs, tmp_path, oracle_lib):
+    """The drop-in's save= file against hackcode1's own savestate/restorestate
+    (code_io.c:222-284 on NEMO's filestruct library, built from the NEMO
+    sources into oracle/_ref): the reference's reader reads every item of it,
+    the reference's writer given those values writes the same bytes, and the
+    drop-in restarts from a state file the reference wrote."""
+    from nemo_gb300 import filestruct as fs
+    O = oracle_lib
+    if not O.state_available():
+        pytest.skip("reference sources not staged (oracle/_ref/libstateref.so absent)")
+    common = ["nbody=512", "seed=7", "freqout=4", "minor_freqout=4", "options=mass,phase,phi,acc"]
+    run(progs, "hackcode1", "out=full.snap", "tstop=1.0", *common, cwd=tmp_path)
+    run(progs, "hackcode1", "out=a.snap", "tstop=0.5", "save=state", *common, cwd=tmp_path)
+    st = O.ref_state_read(tmp_path / "state")
+    a = fs.snapshots(str(tmp_path / "a.snap"))
+    # saved at the last output, after its force evaluation (code_io.c:152-153)
+    assert st["tnow"] == a[-1].time == 0.5 and len(st["mass"]) == 512
+    assert st["freq"] == 32.0 and st["options"] == "mass,phase,phi,acc"
+    assert np.array_equal(st["mass"], a[-1].mass) and np.array_equal(st["phase"], a[-1].phase)
+    assert np.array_equal(st["acc"], a[-1].acc) and np.array_equal(st["phi"], a[-1].phi)
+    O.ref_state_write(tmp_path / "state_ref", st, program="hackcode1", version="1.5b-gb300")
+    assert (tmp_path / "state_ref").read_bytes() == (tmp_path / "state").read_bytes()
+    # a state file written by the reference (its own VERSION) restarts the drop-in
+    O.ref_state_write(tmp_path / "state_nemo", st, program="hackcode1", version="1.5b")
+    run(progs, "hackcode1", "out=b.snap", "restart=state_nemo", "tstop=1.0", "freqout=4", "minor_freqout=4",
+        "options=mass,phase,phi,acc", cwd=tmp_path)
+    full = fs.snapshots(str(tmp_path / "full.snap"))
+    b = fs.snapshots(str(tmp_path / "b.snap"))
+    assert b[-1].time == full[-1].time == 1.0
+    assert np.array_equal(b[-1].phase, full[-1].phase)
 
 
 def test_extension_keywords(progs, tmp_path, oracle_lib):

@@ -1,11 +1,13 @@
 """GPU tests of treecode1's critical-radius criteria (bh86, sw94 and its
 default "new" radius, treecode1/treeload.c:232-252) in the group walk.
 
-treecode1 itself is not built here, so these check the criteria's defining
-properties: accuracy improves as theta shrinks; at one theta the bh86 radius
-is the smallest of the three (size/theta <= both others), so it accepts the
-most; theta = 0 opens every cell (exact direct sum).  Also: the upward pass
-counts each cell's bodies, which the learned criterion's features read."""
+The per-cell radii the walk uses are pinned to treecode1's own setrcrit
+(compiled from the NEMO sources into oracle/_ref/libtc1ref.so) on every cell
+of a GPU tree; the walk is checked by the criteria's defining properties:
+accuracy improves as theta shrinks; at one theta the bh86 radius is the
+smallest of the three (size/theta <= both others), so it accepts the most;
+theta = 0 opens every cell (exact direct sum).  Also: the upward pass counts
+each cell's bodies, which the learned criterion's features read."""
 import numpy as np
 import pytest
 
@@ -98,3 +100,28 @@ def test_small_theta_keeps_the_stack_bounded(hc):
     i2, e2 = _err(ctx, idx, ea)
     assert ctx.walk_stats()["max_stack"] <= 256
     assert e2 < e3 and i2 > i3, (e2, e3, i2, i3)
+
+
+@pytest.mark.parametrize("criterion", ["bh86", "sw94", "barnes"])
+def test_radii_match_treecode1_setrcrit(hc, oracle_lib, criterion):
+    """Every cell's critical radius^2 equals treecode1's setrcrit for the same
+    cell (geometric centre and side from the cell's integer corner and level,
+    FP64 centre of mass from the upward pass) to FP32 rounding."""
+    O = oracle_lib
+    if not O.tc1_available():
+        pytest.skip("reference sources not staged (oracle/_ref/libtc1ref.so absent)")
+    n = 30000
+    m, ph = hc.mkplummer(n, 8)
+    with hc.Context(n, tol=0.5, eps=0.01, usequad=True) as ctx:
+        ctx.upload(m, ph)
+        ctx.build_tree()
+        rmin, rsize = ctx.box()
+        d = ctx.dump_tree()
+        for theta in (0.4, 0.75, 0.0):
+            got = ctx.tree_rcrit(criterion, theta)
+            size = rsize / 2.0 ** d["level"]
+            center = rmin + (d["corner"] + 0.5 * 2.0 ** (30 - d["level"][:, None])) * (rsize / 2.0 ** 30)
+            ref = O.tc1_setrcrit(criterion, theta, rsize, center, size, d["cm"])
+            assert len(got) == len(ref) == len(d["level"])
+            rel = np.abs(got - ref) / ref
+            assert rel.max() <= 1.2e-7, (criterion, theta, rel.max())

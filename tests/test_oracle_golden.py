@@ -189,3 +189,67 @@ def test_oracle_at_1m_against_reference_fixture(oracle_lib):
     acc, phi, n2b, nbc = T.forces(float(g["tol"]), float(g["eps"]), True, idx=idx)
     assert np.array_equal(acc, g["sample_acc"][::8]) and np.array_equal(phi, g["sample_phi"][::8])
     assert np.array_equal(n2b, g["sample_n2b"][::8]) and np.array_equal(nbc, g["sample_nbc"][::8])
+
+
+def test_treecode1_setrcrit_reference_driver(oracle_lib):
+    """treecode1's own setrcrit (treeload.c:232-252), built from the NEMO
+    sources, on random cells: the three criteria's formulas as published in
+    Barnes (1994) / Salmon & Warren (1994) -- (s/theta)^2, bmax^2/theta^2
+    with bmax the largest corner distance from the centre of mass, and
+    (s/theta + |cm - centre|)^2."""
+    O = oracle_lib
+    if not O.tc1_available():
+        pytest.skip("reference sources not present")
+    rng = np.random.default_rng(5)
+    n = 200
+    center = rng.normal(size=(n, 3))
+    size = 2.0 ** rng.integers(-8, 2, n)
+    cm = center + (rng.uniform(-0.5, 0.5, (n, 3)) * size[:, None])
+    th = 0.7
+    np.testing.assert_allclose(O.tc1_setrcrit("bh86", th, 4.0, center, size, cm), (size / th) ** 2, rtol=1e-15)
+    d = cm - center + size[:, None] / 2
+    bmax2 = (np.maximum(d, size[:, None] - d) ** 2).sum(1)
+    np.testing.assert_allclose(O.tc1_setrcrit("sw94", th, 4.0, center, size, cm), bmax2 / th ** 2, rtol=1e-14)
+    off = np.linalg.norm(cm - center, axis=1)
+    np.testing.assert_allclose(O.tc1_setrcrit("barnes", th, 4.0, center, size, cm), (size / th + off) ** 2,
+                               rtol=1e-14)
+    assert np.all(O.tc1_setrcrit("barnes", 0.0, 4.0, center, size, cm) == 64.0)   # theta 0: (2 rsize)^2
+
+
+@pytest.mark.parametrize("kind,pars", [("plummer", [0.0, 2.0, 1.5]), ("hernquist", [0.0, 3.0, 0.5]),
+                                       ("miyamoto", [0.0, 1.0, 0.6, 0.1]), ("log", [0.0, 1.0, 0.8, 0.9, 0.7]),
+                                       ("plummer", [0.0]), ("miyamoto", [0.0, 1.0, 0.0, 0.3])])
+def test_potential_plugins_match_restated_field(oracle_lib, kind, pars):
+    """NEMO's own potential plug-ins (built from the NEMO sources) against the
+    restatement the GPU tests fall back to where those sources are absent."""
+    O = oracle_lib
+    if not O.potential_available(kind):
+        pytest.skip("reference sources not present")
+    from tests.test_gpu_extpot import field
+    x = np.random.default_rng(3).normal(size=(500, 3)) * 2.0
+    ra, rp = O.ref_potential(kind, pars, x)
+    fa, fp = field(kind, pars, x)
+    np.testing.assert_allclose(fa, ra, rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(fp, rp, rtol=1e-12, atol=1e-15)
+
+
+def test_reference_state_file_round_trip(oracle_lib, tmp_path):
+    """hackcode1's own savestate and restorestate (code_io.c:222-284 on NEMO's
+    filestruct library, built from the NEMO sources) round-trip every item."""
+    O = oracle_lib
+    if not O.state_available():
+        pytest.skip("reference sources not present")
+    m, ph = O.mkplummer(300, 4)
+    rng = np.random.default_rng(1)
+    st = dict(freq=32.0, tol=0.7, eps=0.05, fcells=1.0, tstop=2.0, freqout=4.0, minor_freqout=32.0, tnow=0.5,
+              tout=0.75, minor_tout=0.53125, rsize=8.0, headline="state test", options="mass,phi", nstep=16,
+              rmin=np.array([-4.0, -4.0, -4.0]), mass=m, phase=ph, acc=rng.normal(size=(300, 3)),
+              phi=-rng.uniform(size=300))
+    f = tmp_path / "state"
+    O.ref_state_write(f, st)
+    back = O.ref_state_read(f)
+    for k, v in st.items():
+        if isinstance(v, np.ndarray):
+            assert np.array_equal(back[k], v), k
+        else:
+            assert back[k] == v, k
