@@ -175,14 +175,21 @@ def host_cores() -> int:
 
 def cpu_model() -> str:
     try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and v.strip():
+                return f"{v.strip()} ({os.uname().machine})"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
         for line in open("/proc/cpuinfo"):
             k, _, v = line.partition(":")
             if k.strip() in ("model name", "Model"):
                 return v.strip()
-        import platform
-        return platform.processor() or platform.machine()
     except OSError:
-        return "unknown"
+        pass
+    return os.uname().machine
 
 
 class RefWalker:
