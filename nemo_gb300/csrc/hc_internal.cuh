@@ -117,7 +117,7 @@ struct hc_ctx {
     uint32_t *dval[2];
     uint32_t *bfs2pre, *pre2bfs;
     int32_t *parent, *lastc;
-    int32_t *cperm;           // upward pass: cells grouped by depth, then child count
+    int4 *cperm;              // upward pass: cells (index, first child, nodeC.y) grouped by depth, then child count
     uint32_t *cbins;          // their group offsets [257] and placement cursors [256]
     float4 *nodeA, *nodeB, *nodeQ;
     int2 *nodeC;

@@ -565,7 +565,7 @@ __global__ void k_cell_offsets(uint32_t *off, uint32_t *cur)
 
 // places each block's cells: one reservation per group per block, then slots
 // handed out inside the reservation
-__global__ void k_cell_place(const int2 *nodeC, const hc_box *box, uint32_t *cur, int32_t *perm)
+__global__ void k_cell_place(const int2 *nodeC, const hc_box *box, uint32_t *cur, int4 *perm)
 {
     __shared__ uint32_t h[256], base[256];
     const int nn = box->nnode;
@@ -574,8 +574,9 @@ __global__ void k_cell_place(const int2 *nodeC, const hc_box *box, uint32_t *cur
         h[threadIdx.x] = 0;
         __syncthreads();
         int grp = -1, slot = 0;
+        int2 C = make_int2(-1, 0);
         if (k < nn) {
-            const int2 C = nodeC[k];
+            C = nodeC[k];
             if (C.x >= 0 && (C.y & 255) >= 1) {
                 grp = cell_group(C);
                 slot = (int)atomicAdd(&h[grp], 1u);
@@ -584,14 +585,19 @@ __global__ void k_cell_place(const int2 *nodeC, const hc_box *box, uint32_t *cur
         __syncthreads();
         if (h[threadIdx.x]) base[threadIdx.x] = atomicAdd(&cur[threadIdx.x], h[threadIdx.x]);
         __syncthreads();
-        if (grp >= 0) perm[base[grp] + slot] = k;
+        if (grp >= 0) perm[base[grp] + slot] = make_int4(k, C.x, C.y, 0);   // the cell and its child links
         __syncthreads();
     }
 }
 
+__device__ __forceinline__ void prefetch_l1(const void *p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __global__ void __launch_bounds__(256, 2) k_cofm_all(int usequad, const hc_box *box, const int2 *nodeC, double *nm,
                                                      double *ncx, double *ncy, double *ncz, float4 *nodeA,
-                                                     float4 *nodeB, float4 *nodeQ, const int32_t *cperm,
+                                                     float4 *nodeB, float4 *nodeQ, const int4 *cperm,
                                                      const uint32_t *coff)
 {
     cg::grid_group grid = cg::this_grid();
@@ -601,9 +607,17 @@ __global__ void __launch_bounds__(256, 2) k_cofm_all(int usequad, const hc_box *
         const int ls = (int)coff[D * 8], le = (int)coff[D * 8 + 8];
         const float dsqf = __double2float_rn(box->dsq[D]);
         for (int j = ls + (int)grid.thread_rank(); j < le; j += (int)grid.size()) {
-            const int k = cperm[j];
-            const int2 C = nodeC[k];
-            const int fc = C.x, nc = C.y & 255;
+            // the cell with its child links in one load (one dependent round trip less)
+            const int4 P = cperm[j];
+            const int k = P.x, fc = P.y, nc = P.z & 255;
+            // the children's FP32 node data are needed after the FP64 sums: start
+            // bringing their lines into L1 now, beside the FP64 loads
+            prefetch_l1(nodeA + fc);
+            prefetch_l1(nodeA + fc + nc - 1);
+            prefetch_l1(nodeB + fc);
+            prefetch_l1(nodeB + fc + nc - 1);
+            prefetch_l1(nodeQ + 2 * (int64_t)fc);
+            prefetch_l1(nodeQ + 2 * (int64_t)(fc + nc) - 1);
             // The children's loads are issued together (predicated on the
             // child count), not one dependent round trip per child.  FP64 mass
             // and first moments in hackcofm's order (load.c:193-224; bit-exact).
