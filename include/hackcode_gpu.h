@@ -118,6 +118,16 @@ int hc_forces(hc_ctx *ctx);
  * from a CUDA graph captured on the first call (no host round trip inside). */
 int hc_evaluate(hc_ctx *ctx);
 
+/* One force evaluation of host-resident positions, hackforce's per-call
+ * contract (hackforce.c:177-215) with one host round trip: pos [n][3] in
+ * (masses and velocities stay as last uploaded), optionally the previous
+ * evaluation's accelerations prev_acc [n][3] that the error and learned
+ * criteria read (NULL keeps the context's), and acc [n][3] / phi [n] out
+ * (either may be NULL).  The previous accelerations are copied on a stream of
+ * their own while the tree is built; the walk waits for them.  Host buffers
+ * should be page-locked for the copies to run asynchronously. */
+int hc_evaluate_host(hc_ctx *ctx, const double *pos, const double *prev_acc, double *acc, double *phi);
+
 /* CUDA-graph replay of hc_step / hc_evaluate on (1, default) or off (0);
  * results are identical either way. */
 int hc_set_graphs(hc_ctx *ctx, int on);

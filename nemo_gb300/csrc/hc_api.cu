@@ -253,7 +253,12 @@ struct GraphSlot {
 
 struct hc_ctx_ext : hc_ctx {
     Staging stage;
-    GraphSlot graphs[2];          // 0: build + walk, 1: build + walk with closing kick + diagnostics
+    Staging stage_acc;            // hc_evaluate_host: previous accelerations
+    // 0: build + walk, 1: build + walk with closing kick + diagnostics,
+    // 2: build + walk that waits for ev_acc (hc_evaluate_host) before the walk
+    GraphSlot graphs[3];
+    cudaStream_t xfer = nullptr;  // hc_evaluate_host: the previous accelerations' copy, beside the build
+    cudaEvent_t ev_acc = nullptr;
     bool use_graphs = true;
     double *h_diag = nullptr;     // pinned
     double *d_diag = nullptr;
@@ -319,6 +324,12 @@ void hc_destroy(hc_ctx *ctx)
     hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->stage.d) cudaFree(c->stage.d);
+    if (c->stage_acc.d) cudaFree(c->stage_acc.d);
+    if (c->xfer) {
+        cudaStreamSynchronize(c->xfer);
+        cudaStreamDestroy(c->xfer);
+    }
+    if (c->ev_acc) cudaEventDestroy(c->ev_acc);
     if (c->d_diag) cudaFree(c->d_diag);
     if (c->d_idx) cudaFree(c->d_idx);
     if (c->d_out) cudaFree(c->d_out);
@@ -602,7 +613,8 @@ static int fill_diag(hc_ctx_ext *c, hc_diag *d)
 // One force evaluation (build + walk of every body, optional closing kick
 // and diagnostics) enqueued without host synchronisation: the body of both
 // the captured graphs and the direct path.
-static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bool with_diag, bool capturing)
+static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bool with_diag, bool capturing,
+                              cudaEvent_t before_walk = nullptr)
 {
     // inside stream capture an event record must be an explicit graph node
     const unsigned rflags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
@@ -625,6 +637,9 @@ static int enqueue_evaluation(hc_ctx_ext *c, double kick_dthf, int64_t nstep, bo
     }
     if (rb != HC_OK) return rb;
     if (c->criterion >= HC_CRITERION_BH86) hc_rcrit_launch(c, c->criterion - HC_CRITERION_BH86 + 1, c->group_theta);
+    // inputs the walk alone reads (previous accelerations) may arrive beside the build
+    if (before_walk)
+        HC_CUDA(cudaStreamWaitEvent(c->stream, before_walk, capturing ? cudaEventWaitExternal : 0));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, rflags));
     HC_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, rflags));
     HC_TRY(hc_walk_launch(c, true, c->n, c->tord, c->px, c->py, c->pz, c->ax, c->ay, c->az, c->phi, kick_dthf,
@@ -659,12 +674,12 @@ static int finish_evaluation(hc_ctx_ext *c)
 
 // Run an evaluation through a captured CUDA graph (captured on first use,
 // replayed afterwards), or directly when graphs are off.
-static int run_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nstep, bool with_diag)
+static int launch_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nstep, bool with_diag)
 {
+    cudaEvent_t before_walk = slot == 2 ? c->ev_acc : nullptr;
     if (!c->use_graphs) {
         c->launches = 0;
-        HC_TRY(enqueue_evaluation(c, kick_dthf, nstep, with_diag, false));
-        return finish_evaluation(c);
+        return enqueue_evaluation(c, kick_dthf, nstep, with_diag, false, before_walk);
     }
     GraphSlot &g = c->graphs[slot];
     if (!g.exec || g.kick != kick_dthf) {
@@ -673,7 +688,7 @@ static int run_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nst
         cudaGraph_t graph = nullptr;
         HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         c->launches = 0;
-        int r = enqueue_evaluation(c, kick_dthf, nstep, with_diag, true);
+        int r = enqueue_evaluation(c, kick_dthf, nstep, with_diag, true, before_walk);
         cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
         if (r != HC_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -695,6 +710,12 @@ static int run_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nst
     }
     HC_CUDA(cudaGraphLaunch(g.exec, c->stream));
     c->launches = g.launches;
+    return HC_OK;
+}
+
+static int run_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t nstep, bool with_diag)
+{
+    HC_TRY(launch_evaluation(c, slot, kick_dthf, nstep, with_diag));
     return finish_evaluation(c);
 }
 
@@ -708,6 +729,44 @@ int hc_evaluate(hc_ctx *ctx)
 {
     if (!ctx) return HC_ERR_ARG;
     return run_evaluation(static_cast<hc_ctx_ext *>(ctx), 0, 0.0, 0, false);
+}
+
+int hc_evaluate_host(hc_ctx *ctx, const double *pos, const double *prev_acc, double *acc, double *phi)
+{
+    if (!ctx || !pos) return HC_ERR_ARG;
+    hc_ctx_ext *c = static_cast<hc_ctx_ext *>(ctx);
+    const int64_t n = c->n;
+    if (!c->xfer) {
+        if (cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking) != cudaSuccess) {
+            c->xfer = nullptr;
+            c->err = "cudaStreamCreate failed";
+            return HC_ERR_CUDA;
+        }
+        HC_CUDA(cudaEventCreateWithFlags(&c->ev_acc, cudaEventDisableTiming));
+    }
+    HC_TRY(staging(c, c->stage, 3 * n));
+    if (prev_acc) HC_TRY(staging(c, c->stage_acc, 3 * n));
+    // positions: the build needs them first
+    HC_CUDA(cudaMemcpyAsync(c->stage.d, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+    k_unpack3<<<hc_grid(n, 256), 256, 0, c->stream>>>(c->stage.d, n, c->px, c->py, c->pz);
+    // previous accelerations (read by the error and learned criteria in the
+    // walk only): copied on their own stream while the tree is built; the walk
+    // waits for ev_acc.  The previous call ended synchronised, so nothing
+    // still reads the acceleration arrays.
+    if (prev_acc) {
+        HC_CUDA(cudaMemcpyAsync(c->stage_acc.d, prev_acc, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->xfer));
+        k_unpack3<<<hc_grid(n, 256), 256, 0, c->xfer>>>(c->stage_acc.d, n, c->ax, c->ay, c->az);
+        HC_CUDA(cudaEventRecord(c->ev_acc, c->xfer));
+    }
+    c->have_tree = c->have_forces = false;
+    HC_TRY(launch_evaluation(c, 2, 0.0, 0, false));
+    // results out behind the evaluation, one synchronisation for all
+    if (acc) {
+        k_pack3<<<hc_grid(n, 256), 256, 0, c->stream>>>(c->ax, c->ay, c->az, n, c->stage.d, 3, 0);
+        HC_CUDA(cudaMemcpyAsync(acc, c->stage.d, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (phi) HC_CUDA(cudaMemcpyAsync(phi, c->phi, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    return finish_evaluation(c);       // synchronises, then checks the device status
 }
 
 int hc_set_graphs(hc_ctx *ctx, int on)

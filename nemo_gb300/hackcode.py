@@ -28,7 +28,7 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_download",
            "hc_body_counts", "hc_step", "hc_diagnostics", "hc_direct_sample", "hc_last_timing",
            "hc_timer_start", "hc_timer_stop", "hc_fp32_peak", "hc_mkplummer", "hc_mkhernquist", "hc_mkgalaxy", "hc_make_testdata",
-           "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate",
+           "hc_walk_statistics", "hc_set_forces", "hc_snapcopy", "hc_nemo_eval", "hc_evaluate", "hc_evaluate_host",
            "hc_set_graphs", "hc_diagnostics_noalloc", "hc_set_criterion", "hc_set_grouping",
            "hc_learn_nparams", "hc_learn_init", "hc_learn_set_params", "hc_learn_get_params", "hc_learn_infer",
            "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
@@ -126,6 +126,7 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_tree_rcrit.argtypes = [_vp, C.c_int, C.c_double, _dp]
     L.hc_forces.argtypes = [_vp]
     L.hc_evaluate.argtypes = [_vp]
+    L.hc_evaluate_host.argtypes = [_vp, _vp, _vp, _vp, _vp]
     L.hc_set_criterion.argtypes = [_vp, C.c_int, C.c_double]
     L.hc_set_grouping.argtypes = [_vp, C.c_int]
     L.hc_set_guard.argtypes = [_vp, C.c_int64, C.c_double, C.c_uint64]
@@ -459,6 +460,20 @@ class Context:
     def evaluate(self):
         """build_tree + forces as one CUDA-graph replay."""
         self._check(self._L.hc_evaluate(self._h))
+
+    def evaluate_host_ptr(self, pos_ptr: int, prev_acc_ptr=None, acc_ptr=None, phi_ptr=None):
+        """hc_evaluate_host on raw host pointers (page-locked buffers): positions [n][3] in, optionally the
+        previous accelerations [n][3] in, accelerations [n][3] / potentials [n] out."""
+        self._check(self._L.hc_evaluate_host(self._h, pos_ptr, prev_acc_ptr, acc_ptr, phi_ptr))
+
+    def evaluate_host(self, pos, prev_acc=None, acc=True, phi=True):
+        """hc_evaluate_host on numpy arrays: returns (acc[n,3] or None, phi[n] or None)."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(self.n, 3)
+        pa = None if prev_acc is None else np.ascontiguousarray(prev_acc, dtype=np.float64).reshape(self.n, 3)
+        a = np.zeros((self.n, 3)) if acc else None
+        f = np.zeros(self.n) if phi else None
+        self._check(self._L.hc_evaluate_host(self._h, _ptr(p), _ptr(pa), _ptr(a), _ptr(f)))
+        return a, f
 
     def set_graphs(self, on: bool):
         self._check(self._L.hc_set_graphs(self._h, int(bool(on))))

@@ -214,3 +214,38 @@ def test_many_test_points_keep_the_captured_graphs(hc):
     # the FP32 sums agree to rounding, not bit for bit
     assert _rel(acc2, acc[:5000]).max() < 1e-5
     assert (np.abs(phi2 - phi[:5000]) / np.abs(phi[:5000])).max() < 1e-5
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+@pytest.mark.parametrize("crit", [("body", 0.0), ("error", 0.05), ("learned", 0.05)])
+def test_evaluate_host_matches_the_device_path(hc, graphs, crit):
+    """hc_evaluate_host (positions and previous accelerations from the host,
+    the latter copied beside the build; results back in one round trip) gives
+    the same bits as hc_upload + hc_set_forces + hc_evaluate + hc_download."""
+    n = 20000
+    m, ph = hc.mkplummer(n, 3)
+    ph2 = ph.copy()
+    ph2[:, 0] += 0.01 * ph[:, 1]                       # the next positions
+    out = []
+    for host in (False, True):
+        with hc.Context(n, tol=0.5, eps=0.01, usequad=True) as ctx:
+            ctx.set_graphs(graphs)
+            ctx.upload(m, ph)
+            if crit[0] == "learned":
+                ctx.learn_init(3)                          # an untrained network still decides the band
+            ctx.set_criterion(*crit)
+            ctx.evaluate()                                 # same box history in both paths
+            _, a_prev, _ = ctx.download(phase=False, phi=False)
+            if host:
+                a, p = ctx.evaluate_host(ph2[:, 0], prev_acc=a_prev)
+                a2, p2 = ctx.evaluate_host(ph2[:, 0])       # keeps the accelerations it computed
+            else:
+                ctx.upload(m, ph2)
+                ctx.set_forces(a_prev)
+                ctx.evaluate()
+                _, a, p = ctx.download(phase=False)
+                ctx.evaluate()
+                _, a2, p2 = ctx.download(phase=False)
+            out.append((a, p, a2, p2))
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
