@@ -690,6 +690,7 @@ def run_ensemble(args, world, rank, local):
     ens = hc.Ensemble(counts, tol=ENS_TOL, eps=ENS_EPS, usequad=False, direct_max=ENS_DIRECT_MAX)
     ens.upload(m, ph)
     e0 = ens.step(ENS_DT, 0, energy=True)
+    tuning = ens.autotune()                  # walk groups and direct-sum block size, timed on these bodies
     for k in range(1, args.warmup + 1):
         ens.step(ENS_DT, k)
     barrier(world)
@@ -719,6 +720,7 @@ def run_ensemble(args, world, rank, local):
                    "(each step is one CUDA-graph launch followed by a stream synchronisation)"},
         "gpu_launches": inf["launches"] * args.steps,
         "phase_ms": {"tree": statistics.mean(tree_ms), "direct": statistics.mean(direct_ms)},
+        "tuning": tuning,
         "systems": {"tree": inf["nsys_tree"], "direct": inf["nsys_direct"], "bodies_tree": inf["bodies_tree"],
                     "bodies_direct": inf["bodies_direct"]},
         "interactions_per_s": (inf["interactions_tree"] + inf["interactions_direct"]) / (mean_ms * 1e-3),

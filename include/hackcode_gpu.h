@@ -405,6 +405,20 @@ int hc_ens_upload(hc_ens *e, const double *mass, const double *phase);
 int hc_ens_step(hc_ens *e, double dt, int64_t nstep, double *energy);
 int hc_ens_download(hc_ens *e, double *phase, double *acc, double *phi);
 int hc_ens_info(hc_ens *e, hc_ens_stats *out);
+/* Tuning of an ensemble's step (no counterpart in the reference): the tree
+ * systems' walk groups (group_max 1..64 bodies, list_depth 32..64; always
+ * tree-aligned) and the direct sum's block size (128, 256 or 512 threads).
+ * hc_ens_autotune times the two force phases for every candidate on the
+ * current bodies (after hc_ens_upload; positions, velocities, accelerations
+ * and potentials are left as they were) and keeps the fastest; tree_ms /
+ * direct_ms are the winners' phase times. */
+typedef struct {
+    int group_max, list_depth, direct_threads;
+    double tree_ms, direct_ms;
+} hc_ens_tuning;
+int hc_ens_set_tuning(hc_ens *e, const hc_ens_tuning *t);
+int hc_ens_get_tuning(hc_ens *e, hc_ens_tuning *t);
+int hc_ens_autotune(hc_ens *e, hc_ens_tuning *best);
 
 #ifdef __cplusplus
 }

@@ -44,7 +44,7 @@
 
 namespace {
 
-constexpr int DTHREADS = 256;
+constexpr int DTHREADS = 256;       // energy kernel; the direct sum's block size is tuned (128..512)
 
 struct SysBox {
     double rmin[3];
@@ -201,8 +201,9 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float x)
 }
 
 // 5. direct sum of one small system per block (FP32, hi + lo positions
-// relative to the system's first body; Kahan over 64-body partials)
-__global__ void __launch_bounds__(DTHREADS) k_ens_direct(const int32_t *dsys, const int64_t *off, const double *mass,
+// relative to the system's first body; Kahan over 64-body partials); any
+// block size up to 512 threads
+__global__ void __launch_bounds__(512) k_ens_direct(const int32_t *dsys, const int64_t *off, const double *mass,
                                                          const double *px, const double *py, const double *pz,
                                                          float eps2, double kick_dthf, int64_t nstep, double *vx,
                                                          double *vy, double *vz, double *ax, double *ay, double *az,
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(DTHREADS) k_ens_direct(const int32_t *dsys, co
     const int n = (int)(off[s + 1] - b0);
     float4 *H = sm, *L = sm + n;
     const double cx = px[b0], cy = py[b0], cz = pz[b0];
-    for (int j = threadIdx.x; j < n; j += DTHREADS) {
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
         const double dx = px[b0 + j] - cx, dy = py[b0 + j] - cy, dz = pz[b0 + j] - cz;
         const float hx = __double2float_rn(dx), hy = __double2float_rn(dy), hz = __double2float_rn(dz);
         H[j] = make_float4(hx, hy, hz, __double2float_rn(mass[b0 + j]));
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(DTHREADS) k_ens_direct(const int32_t *dsys, co
                            __double2float_rn(dz - (double)hz), 0.f);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += DTHREADS) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 Hi = H[i], Li = L[i];
         float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, cxs = 0.f, cys = 0.f, czs = 0.f, cps = 0.f;
         for (int j0 = 0; j0 < n; j0 += 64) {
@@ -367,6 +368,7 @@ struct hc_ens {
     SysBox *d_box = nullptr;
     double *d_origin = nullptr, *d_energy = nullptr, *h_energy = nullptr, *d_stage = nullptr;
     int max_direct_n = 0;
+    int direct_threads = 256;                    // block size of the direct sum (tuned)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     double graph_dt[2] = {0.0, 0.0};
     int64_t launches = 0, graph_launches[2] = {0, 0};
@@ -386,7 +388,7 @@ namespace {
 
 // Everything of one step after the positions are final, on e->stream,
 // without host synchronisation (graph-capturable).
-int ens_enqueue(hc_ens *e, double kick_dthf, int64_t nstep, double dt, bool capturing)
+int ens_enqueue(hc_ens *e, double kick_dthf, int64_t nstep, double dt, bool capturing, bool advance = true)
 {
     cudaStream_t s = e->stream;
     const unsigned rflags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
@@ -421,12 +423,13 @@ int ens_enqueue(hc_ens *e, double kick_dthf, int64_t nstep, double dt, bool capt
     EC(cudaEventRecordWithFlags(e->ev[1], s, rflags));
     if (e->nsys_direct > 0) {
         const size_t smem = sizeof(float4) * 2 * (size_t)e->max_direct_n;
-        k_ens_direct<<<e->nsys_direct, DTHREADS, smem, s>>>(e->d_dsys, e->d_off, e->mass, e->px, e->py, e->pz,
+        k_ens_direct<<<e->nsys_direct, e->direct_threads, smem, s>>>(e->d_dsys, e->d_off, e->mass, e->px, e->py, e->pz,
                                                              (float)(e->prm.eps * e->prm.eps), kick_dthf, nstep,
                                                              e->vx, e->vy, e->vz, e->ax, e->ay, e->az, e->phi);
         e->launches++;
     }
     EC(cudaEventRecordWithFlags(e->ev[2], s, rflags));
+    if (!advance) return HC_OK;          // forces only (the autotuner's evaluations)
     k_ens_energy<<<e->nsys, DTHREADS, 0, s>>>(e->d_off, e->d_user_of, e->mass, e->vx, e->vy, e->vz, e->phi,
                                               e->d_energy);
     k_ens_kick_drift<<<hc_grid(e->ntot, 256), 256, 0, s>>>(e->ntot, dt, e->px, e->py, e->pz, e->vx, e->vy, e->vz,
@@ -655,6 +658,125 @@ int hc_ens_step(hc_ens *e, double dt, int64_t nstep, double *energy)
     EC(cudaEventElapsedTime(&e->tree_ms, e->ev[0], e->ev[1]));
     EC(cudaEventElapsedTime(&e->direct_ms, e->ev[1], e->ev[2]));
     if (energy) std::memcpy(energy, e->h_energy, sizeof(double) * 3 * e->nsys);
+    return HC_OK;
+}
+
+int hc_ens_set_tuning(hc_ens *e, const hc_ens_tuning *t)
+{
+    if (!e || !t) return HC_ERR_ARG;
+    if (t->direct_threads != 128 && t->direct_threads != 256 && t->direct_threads != 512) {
+        e->err = "hc_ens_set_tuning: direct_threads 128, 256 or 512";
+        return HC_ERR_ARG;
+    }
+    if (e->forest) {
+        hc_tuning w{t->group_max, t->list_depth, HC_GROUPS_TREE, 0.0};   // forest groups never straddle systems
+        int r = hc_set_tuning(e->forest, &w);
+        if (r != HC_OK) {
+            e->err = std::string("forest: ") + e->forest->err;
+            return r;
+        }
+    }
+    e->direct_threads = t->direct_threads;
+    for (int k = 0; k < 2; k++)
+        if (e->graph[k]) {
+            cudaGraphExecDestroy(e->graph[k]);
+            e->graph[k] = nullptr;
+        }
+    return HC_OK;
+}
+
+int hc_ens_get_tuning(hc_ens *e, hc_ens_tuning *t)
+{
+    if (!e || !t) return HC_ERR_ARG;
+    hc_tuning w{HC_GROUP2, 64, HC_GROUPS_TREE, 0.0};
+    if (e->forest) hc_get_tuning(e->forest, &w);
+    t->group_max = w.group_max;
+    t->list_depth = w.list_depth;
+    t->direct_threads = e->direct_threads;
+    t->tree_ms = t->direct_ms = 0.0;
+    return HC_OK;
+}
+
+// Times the force phases (tree systems, direct systems) of the current bodies
+// for each candidate and keeps the fastest.  Positions and velocities do not
+// move; the accelerations and potentials the step in progress needs are
+// restored afterwards.
+int hc_ens_autotune(hc_ens *e, hc_ens_tuning *best)
+{
+    if (!e) return HC_ERR_ARG;
+    if (!e->d_stage) {
+        e->err = "hc_ens_autotune: upload the bodies first";
+        return HC_ERR_STATE;
+    }
+    const int64_t n = e->ntot;
+    const size_t b = sizeof(double) * (size_t)n;
+    double *const keep[4] = {e->ax, e->ay, e->az, e->phi};
+    for (int k = 0; k < 4; k++) EC(cudaMemcpyAsync(e->d_stage + k * n, keep[k], b, cudaMemcpyDeviceToDevice, e->stream));
+    hc_ens_tuning cur;
+    hc_ens_get_tuning(e, &cur);
+    auto timed = [&](const hc_ens_tuning &t, double *tree, double *direct) -> int {
+        HC_TRY(hc_ens_set_tuning(e, &t));
+        *tree = *direct = 1e300;
+        for (int rep = 0; rep < 3; rep++) {
+            HC_TRY(ens_enqueue(e, 0.0, 0, 0.0, false, false));
+            EC(cudaStreamSynchronize(e->stream));
+            if (e->forest) {
+                EC(cudaMemcpy(e->forest->h_st, e->forest->st, sizeof(hc_status), cudaMemcpyDeviceToHost));
+                if (e->forest->h_st->error) {
+                    e->err = std::string("ensemble autotune: ") + status_text(e->forest->h_st->error);
+                    return e->forest->h_st->error;
+                }
+            }
+            float t0 = 0.f, t1 = 0.f;
+            EC(cudaEventElapsedTime(&t0, e->ev[0], e->ev[1]));
+            EC(cudaEventElapsedTime(&t1, e->ev[1], e->ev[2]));
+            *tree = std::min(*tree, (double)t0);
+            *direct = std::min(*direct, (double)t1);
+        }
+        return HC_OK;
+    };
+    hc_ens_tuning win = cur;
+    win.tree_ms = win.direct_ms = 1e300;
+    int r = HC_OK;
+    // the two phases are independent: tree tuning first, then the direct block size
+    const int gms[] = {HC_GROUP2 / 2, 3 * HC_GROUP2 / 4, HC_GROUP2}, lds[] = {32, 48, 64}, dts[] = {128, 256, 512};
+    for (int gm : gms) {
+        if (!e->forest && gm != cur.group_max) continue;
+        for (int ld : lds) {
+            if (!e->forest && ld != cur.list_depth) continue;
+            hc_ens_tuning t{gm, ld, cur.direct_threads, 0.0, 0.0};
+            double tr, di;
+            if ((r = timed(t, &tr, &di)) != HC_OK) break;
+            if (tr < win.tree_ms) {
+                win.group_max = gm;
+                win.list_depth = ld;
+                win.tree_ms = tr;
+            }
+        }
+        if (r != HC_OK) break;
+    }
+    for (int dt : dts) {
+        if (r != HC_OK || e->nsys_direct == 0) break;
+        hc_ens_tuning t{win.group_max, win.list_depth, dt, 0.0, 0.0};
+        double tr, di;
+        if ((r = timed(t, &tr, &di)) != HC_OK) break;
+        if (di < win.direct_ms) {
+            win.direct_threads = dt;
+            win.direct_ms = di;
+        }
+    }
+    for (int k = 0; k < 4; k++) EC(cudaMemcpyAsync(keep[k], e->d_stage + k * n, b, cudaMemcpyDeviceToDevice, e->stream));
+    EC(cudaStreamSynchronize(e->stream));
+    if (r != HC_OK) {                        // keep the caller's tuning and the error message
+        const std::string err = e->err;
+        hc_ens_set_tuning(e, &cur);
+        e->err = err;
+        return r;
+    }
+    HC_TRY(hc_ens_set_tuning(e, &win));
+    if (e->nsys_direct == 0) win.direct_ms = 0.0;
+    if (!e->forest) win.tree_ms = 0.0;
+    if (best) *best = win;
     return HC_OK;
 }
 

@@ -43,6 +43,7 @@ __global__ void k_mlp_infer(const MlpSmem *params, const float *x, int64_t n, fl
 {
     __shared__ MlpSmem P;
     __shared__ __nv_bfloat16 tile[4][32 * MLP_XS];
+    __shared__ float zbuf[4][32];
     mlp_load(P, params);
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -50,7 +51,7 @@ __global__ void k_mlp_infer(const MlpSmem *params, const float *x, int64_t n, fl
     for (int k = 0; k < MLP_XS; k++)
         tile[w][lane * MLP_XS + k] = __float2bfloat16_rn((row < n && k < MLP_IN) ? x[row * MLP_IN + k] : 0.f);
     __syncwarp();
-    const float z = mlp_warp32(P, tile[w]);
+    const float z = mlp_warp_lean(P, tile[w], zbuf[w], 32);     // the walk's network round
     if (row < n) logits[row] = z;
 }
 

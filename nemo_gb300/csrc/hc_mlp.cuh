@@ -20,7 +20,7 @@
 #define MLP_S2 72            // row stride (bf16) of w2t / w3t
 #define MLP_XS 24            // row stride (bf16) of a 32 x 16 input tile
 
-struct MlpSmem {
+struct __align__(16) MlpSmem {     // 16-byte aligned: ldmatrix row addresses
     __nv_bfloat16 w1t[MLP_H * MLP_S1];
     __nv_bfloat16 w2t[MLP_H * MLP_S2];
     __nv_bfloat16 w3t[8 * MLP_S2];
@@ -73,112 +73,41 @@ __device__ __forceinline__ void mlp_load(MlpSmem &dst, const MlpSmem *src)
     for (int i = threadIdx.x; i < (int)(sizeof(MlpSmem) / 4); i += blockDim.x) d[i] = s[i];
 }
 
-// Logits of MT * 16 rows (MT = 1 or 2).  x: this warp's 32 x MLP_XS bf16
-// input tile (row r = lane r's candidate, columns 12..15 zero).  Returns the
-// logit of row `lane` (rows >= MT * 16: undefined).  The two m-tiles share
-// every weight-fragment load.  Callers keep it out of line (mlp_warp32, or a
-// non-inlined caller of their own): its fragments would otherwise raise the
-// register count of the code around it.
-template <int MT>
-__device__ __forceinline__ float mlp_warp(const MlpSmem &P, const __nv_bfloat16 *x)
+// Four 8x8 bf16 matrices from shared memory in one instruction (PTX
+// ldmatrix): lane i gives the row address of row i % 8 of matrix i / 8 and
+// receives r[m] = elements 2 (i % 4), +1 of row i / 4 of matrix m -- for a
+// weight stored as W^T[n][k] that is the B fragment (n = g, k = 2t, 2t+1) of
+// mma.m16n8k16.  Row addresses must be 16-byte aligned.
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const __nv_bfloat16 *row)
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const uint32_t *xw = reinterpret_cast<const uint32_t *>(x);
-    const uint32_t *w1 = reinterpret_cast<const uint32_t *>(P.w1t);
-    const uint32_t *w2 = reinterpret_cast<const uint32_t *>(P.w2t);
-    const uint32_t *w3 = reinterpret_cast<const uint32_t *>(P.w3t);
-    // ---- layer 1: [16 x 16] x [16 x 64] per m-tile ----
-    uint32_t a[MT][4];
-#pragma unroll
-    for (int mt = 0; mt < MT; mt++) {
-        const int r0 = mt * 16;
-        a[mt][0] = xw[((r0 + g) * MLP_XS + 2 * t) >> 1];
-        a[mt][1] = xw[((r0 + g + 8) * MLP_XS + 2 * t) >> 1];
-        a[mt][2] = xw[((r0 + g) * MLP_XS + 2 * t + 8) >> 1];
-        a[mt][3] = xw[((r0 + g + 8) * MLP_XS + 2 * t + 8) >> 1];
-    }
-    uint32_t h1[MT][4][4];                   // layer-1 activations as layer-2 A fragments (k-tiles 0..3)
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int n = nt * 8 + g, col = nt * 8 + 2 * t;
-        const uint32_t b0 = w1[(n * MLP_S1 + 2 * t) >> 1], b1 = w1[(n * MLP_S1 + 2 * t + 8) >> 1];
-        const float bias0 = P.b1[col], bias1 = P.b1[col + 1];
-#pragma unroll
-        for (int mt = 0; mt < MT; mt++) {
-            float c[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_bf16_16816(c, a[mt], b0, b1);
-            const int kt = nt >> 1, half = nt & 1;
-            h1[mt][kt][half * 2 + 0] = pack_bf16(silu(c[0] + bias0), silu(c[1] + bias1));   // row g
-            h1[mt][kt][half * 2 + 1] = pack_bf16(silu(c[2] + bias0), silu(c[3] + bias1));   // row g + 8
-        }
-    }
-    // ---- layer 2: [16 x 64] x [64 x 64], then layer 3 on the fly ----
-    float c3[MT][4], hold[MT][4];
-#pragma unroll
-    for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) c3[mt][q] = hold[mt][q] = 0.f;
-#pragma unroll 2
-    for (int nt = 0; nt < 8; nt++) {
-        const int n = nt * 8 + g, col = nt * 8 + 2 * t;
-        uint32_t b[4][2];
-#pragma unroll
-        for (int kt = 0; kt < 4; kt++) {
-            b[kt][0] = w2[(n * MLP_S2 + kt * 16 + 2 * t) >> 1];
-            b[kt][1] = w2[(n * MLP_S2 + kt * 16 + 2 * t + 8) >> 1];
-        }
-        const float bias0 = P.b2[col], bias1 = P.b2[col + 1];
-        uint32_t w3b0 = 0u, w3b1 = 0u;
-        if (nt & 1) {
-            const int kt = nt >> 1;
-            w3b0 = w3[(g * MLP_S2 + kt * 16 + 2 * t) >> 1];
-            w3b1 = w3[(g * MLP_S2 + kt * 16 + 2 * t + 8) >> 1];
-        }
-#pragma unroll
-        for (int mt = 0; mt < MT; mt++) {
-            float c[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int kt = 0; kt < 4; kt++) mma_bf16_16816(c, h1[mt][kt], b[kt][0], b[kt][1]);
-            const float v0 = silu(c[0] + bias0), v1 = silu(c[1] + bias1);
-            const float v2 = silu(c[2] + bias0), v3 = silu(c[3] + bias1);
-            // layer 3 consumes k-tile nt/2 of the layer-2 output when both halves are ready
-            if (nt & 1) {
-                // A fragment: rows g / g+8 of n-tiles nt-1 (held) and nt
-                const uint32_t af[4] = {pack_bf16(hold[mt][0], hold[mt][1]), pack_bf16(hold[mt][2], hold[mt][3]),
-                                        pack_bf16(v0, v1), pack_bf16(v2, v3)};
-                mma_bf16_16816(c3[mt], af, w3b0, w3b1);
-            } else {
-                hold[mt][0] = v0;
-                hold[mt][1] = v1;
-                hold[mt][2] = v2;
-                hold[mt][3] = v3;
-            }
-        }
-    }
-    // column 0 of c3 (t == 0 lanes) holds rows g and g + 8 of each m-tile.
-    // Lane r wants row r: rows (r&7) and (r&7)+8 of its m-tile sit in lane 4 (r&7).
-    const int rr = lane & 15, src_lane = (rr & 7) * 4;
-    const float a0 = __shfl_sync(0xffffffffu, c3[0][0], src_lane), a1 = __shfl_sync(0xffffffffu, c3[0][2], src_lane);
-    float v = rr < 8 ? a0 : a1;
-    if (MT == 2) {
-        const float b0 = __shfl_sync(0xffffffffu, c3[MT - 1][0], src_lane);
-        const float b1 = __shfl_sync(0xffffffffu, c3[MT - 1][2], src_lane);
-        if (lane >= 16) v = rr < 8 ? b0 : b1;
-    }
-    return v + P.b3;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(row);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
 }
 
-// Register-lean form of mlp_warp for use inline in a register-heavy kernel:
-// one m-tile at a time, weight fragments loaded per use; the logits pass
-// through z[32] (shared memory of the warp).  Rows >= nrows are skipped in
-// 16-row steps.
+// silu of a pair of values: the products and sums in packed FP32x2 (each half
+// rounded as the scalar instruction would), the tanh per value
+__device__ __forceinline__ float2 silu2(float2 x)
+{
+    const float2 h = __fmul2_rn(x, make_float2(0.5f, 0.5f));
+    return __ffma2_rn(h, make_float2(tanh_fast(h.x), tanh_fast(h.y)), h);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16_2(float2 v) { return pack_bf16(v.x, v.y); }
+
+// Logits of the rows of x, for use inline in a register-heavy kernel: one
+// 16-row m-tile at a time (rows >= nrows are skipped in 16-row steps), weight
+// fragments loaded per use with ldmatrix, biases as the accumulators' initial
+// values, activations in packed FP32x2; the logits pass through z[32]
+// (shared memory of the warp).  x: this warp's 32 x MLP_XS bf16 input tile
+// (row r = lane r's candidate, columns 12..15 zero).  Returns the logit of row
+// `lane`.
 __device__ __forceinline__ float mlp_warp_lean(const MlpSmem &P, const __nv_bfloat16 *x, float *z, int nrows)
 {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int lr = lane & 7, lm = lane >> 3;     // ldmatrix: row and matrix this lane addresses
     const uint32_t *xw = reinterpret_cast<const uint32_t *>(x);
-    const uint32_t *w1 = reinterpret_cast<const uint32_t *>(P.w1t);
-    const uint32_t *w2 = reinterpret_cast<const uint32_t *>(P.w2t);
-    const uint32_t *w3 = reinterpret_cast<const uint32_t *>(P.w3t);
     const int nmt = nrows <= 16 ? 1 : 2;
 #pragma unroll 1
     for (int mt = 0; mt < nmt; mt++) {
@@ -188,47 +117,50 @@ __device__ __forceinline__ float mlp_warp_lean(const MlpSmem &P, const __nv_bflo
         a[1] = xw[((r0 + g + 8) * MLP_XS + 2 * t) >> 1];
         a[2] = xw[((r0 + g) * MLP_XS + 2 * t + 8) >> 1];
         a[3] = xw[((r0 + g + 8) * MLP_XS + 2 * t + 8) >> 1];
-        uint32_t h1[4][4];
+        // ---- layer 1: [16 x 16] x [16 x 64], two n-tiles per ldmatrix ----
+        uint32_t h1[4][4];                   // activations as layer-2 A fragments (k-tiles 0..3)
 #pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const int n = nt * 8 + g, col = nt * 8 + 2 * t;
-            float c[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_bf16_16816(c, a, w1[(n * MLP_S1 + 2 * t) >> 1], w1[(n * MLP_S1 + 2 * t + 8) >> 1]);
-            const float bias0 = P.b1[col], bias1 = P.b1[col + 1];
-            const int kt = nt >> 1, half = nt & 1;
-            h1[kt][half * 2 + 0] = pack_bf16(silu(c[0] + bias0), silu(c[1] + bias1));
-            h1[kt][half * 2 + 1] = pack_bf16(silu(c[2] + bias0), silu(c[3] + bias1));
+        for (int np = 0; np < 4; np++) {
+            uint32_t b[4];                   // n-tiles 2np, 2np+1: (k 0-7, k 8-15) each
+            ldsm_x4(b, P.w1t + (16 * np + 8 * (lm >> 1) + lr) * MLP_S1 + 8 * (lm & 1));
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int col = (2 * np + hh) * 8 + 2 * t;
+                const float2 bias = make_float2(P.b1[col], P.b1[col + 1]);
+                float c[4] = {bias.x, bias.y, bias.x, bias.y};
+                mma_bf16_16816(c, a, b[2 * hh], b[2 * hh + 1]);
+                h1[np][hh * 2 + 0] = pack_bf16_2(silu2(make_float2(c[0], c[1])));   // row g
+                h1[np][hh * 2 + 1] = pack_bf16_2(silu2(make_float2(c[2], c[3])));   // row g + 8
+            }
         }
+        // ---- layer 2: [16 x 64] x [64 x 64], then layer 3 on the fly ----
         float c3[4] = {0.f, 0.f, 0.f, 0.f};
-        float hold[4] = {0.f, 0.f, 0.f, 0.f};
+        float2 hold0 = make_float2(0.f, 0.f), hold1 = hold0;
 #pragma unroll 2
         for (int nt = 0; nt < 8; nt++) {
-            const int n = nt * 8 + g, col = nt * 8 + 2 * t;
+            const int col = nt * 8 + 2 * t;
+            uint32_t b01[4], b23[4];         // k-tiles 0,1 and 2,3 of n-tile nt
+            ldsm_x4(b01, P.w2t + (8 * nt + lr) * MLP_S2 + 8 * lm);
+            ldsm_x4(b23, P.w2t + (8 * nt + lr) * MLP_S2 + 32 + 8 * lm);
             // k-tiles 0,1 and 2,3 in two independent accumulators (shorter mma chain)
-            float c[4] = {0.f, 0.f, 0.f, 0.f}, e[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int kt = 0; kt < 2; kt++) {
-                mma_bf16_16816(c, h1[kt], w2[(n * MLP_S2 + kt * 16 + 2 * t) >> 1],
-                               w2[(n * MLP_S2 + kt * 16 + 2 * t + 8) >> 1]);
-                mma_bf16_16816(e, h1[kt + 2], w2[(n * MLP_S2 + (kt + 2) * 16 + 2 * t) >> 1],
-                               w2[(n * MLP_S2 + (kt + 2) * 16 + 2 * t + 8) >> 1]);
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) c[q] += e[q];
-            const float bias0 = P.b2[col], bias1 = P.b2[col + 1];
-            const float v0 = silu(c[0] + bias0), v1 = silu(c[1] + bias1);
-            const float v2 = silu(c[2] + bias0), v3 = silu(c[3] + bias1);
+            const float2 bias = make_float2(P.b2[col], P.b2[col + 1]);
+            float c[4] = {bias.x, bias.y, bias.x, bias.y}, e[4] = {0.f, 0.f, 0.f, 0.f};
+            mma_bf16_16816(c, h1[0], b01[0], b01[1]);
+            mma_bf16_16816(e, h1[2], b23[0], b23[1]);
+            mma_bf16_16816(c, h1[1], b01[2], b01[3]);
+            mma_bf16_16816(e, h1[3], b23[2], b23[3]);
+            const float2 v01 = silu2(__fadd2_rn(make_float2(c[0], c[1]), make_float2(e[0], e[1])));
+            const float2 v23 = silu2(__fadd2_rn(make_float2(c[2], c[3]), make_float2(e[2], e[3])));
             if (nt & 1) {
                 const int kt = nt >> 1;
-                const uint32_t af[4] = {pack_bf16(hold[0], hold[1]), pack_bf16(hold[2], hold[3]), pack_bf16(v0, v1),
-                                        pack_bf16(v2, v3)};
+                // A fragment: rows g / g+8 of n-tiles nt-1 (held) and nt
+                const uint32_t af[4] = {pack_bf16_2(hold0), pack_bf16_2(hold1), pack_bf16_2(v01), pack_bf16_2(v23)};
+                const uint32_t *w3 = reinterpret_cast<const uint32_t *>(P.w3t);
                 mma_bf16_16816(c3, af, w3[(g * MLP_S2 + kt * 16 + 2 * t) >> 1],
                                w3[(g * MLP_S2 + kt * 16 + 2 * t + 8) >> 1]);
             } else {
-                hold[0] = v0;
-                hold[1] = v1;
-                hold[2] = v2;
-                hold[3] = v3;
+                hold0 = v01;
+                hold1 = v23;
             }
         }
         if (t == 0) {                        // column 0: rows g and g + 8 of this m-tile
@@ -242,8 +174,3 @@ __device__ __forceinline__ float mlp_warp_lean(const MlpSmem &P, const __nv_bflo
     return v;
 }
 
-// Logits of the 32 rows of x (see mlp_warp); rows < nrows are needed.
-static __device__ __noinline__ float mlp_warp32(const MlpSmem &P, const __nv_bfloat16 *x, int nrows = 32)
-{
-    return nrows <= 16 ? mlp_warp<1>(P, x) : mlp_warp<2>(P, x);
-}

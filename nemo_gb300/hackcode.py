@@ -34,7 +34,7 @@ EXPORTS = ["hc_create", "hc_destroy", "hc_last_error", "hc_set_params", "hc_uplo
            "hc_learn_gradient", "hc_learn_collect", "hc_learn_samples", "hc_learn_load_samples", "hc_learn_train",
            "hc_learn_set_threshold", "hc_learn_relabel", "hc_learn_set_band", "hc_set_guard", "hc_guard_stats",
            "hc_ens_create", "hc_ens_destroy", "hc_ens_last_error", "hc_ens_upload", "hc_ens_step",
-           "hc_ens_download", "hc_ens_info", "hc_set_tuning", "hc_get_tuning", "hc_autotune", "hc_set_extpot",
+           "hc_ens_download", "hc_ens_info", "hc_ens_set_tuning", "hc_ens_get_tuning", "hc_ens_autotune", "hc_set_tuning", "hc_get_tuning", "hc_autotune", "hc_set_extpot",
            "hc_generate"]
 
 
@@ -72,6 +72,14 @@ class Tuning(C.Structure):
     def as_dict(self):
         return {"group_max": self.group_max, "list_depth": self.list_depth,
                 "grouping": ["consecutive", "tree"][self.grouping], "ms": self.ms}
+
+
+class EnsTuning(C.Structure):
+    _fields_ = [("group_max", C.c_int), ("list_depth", C.c_int), ("direct_threads", C.c_int),
+                ("tree_ms", C.c_double), ("direct_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class EnsParams(C.Structure):
@@ -144,6 +152,9 @@ def library(build_if_missing: bool = False) -> C.CDLL:
     L.hc_ens_step.argtypes = [_vp, C.c_double, C.c_int64, _vp]
     L.hc_ens_download.argtypes = [_vp, _vp, _vp, _vp]
     L.hc_ens_info.argtypes = [_vp, C.POINTER(EnsStats)]
+    L.hc_ens_set_tuning.argtypes = [_vp, C.POINTER(EnsTuning)]
+    L.hc_ens_get_tuning.argtypes = [_vp, C.POINTER(EnsTuning)]
+    L.hc_ens_autotune.argtypes = [_vp, C.POINTER(EnsTuning)]
     L.hc_guard_stats.argtypes = [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
     L.hc_learn_nparams.argtypes = []
@@ -575,6 +586,22 @@ class Ensemble:
         p = np.zeros(self.n) if phi else None
         self._check(self._L.hc_ens_download(self._h, _ptr(ph), _ptr(a), _ptr(p)))
         return ph, a, p
+
+    def set_tuning(self, group_max=64, list_depth=64, direct_threads=256):
+        t = EnsTuning(int(group_max), int(list_depth), int(direct_threads), 0.0, 0.0)
+        self._check(self._L.hc_ens_set_tuning(self._h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = EnsTuning()
+        self._check(self._L.hc_ens_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def autotune(self) -> dict:
+        """Fastest walk groups for the tree systems and block size for the direct sums, timed on the
+        current bodies (nothing moves)."""
+        t = EnsTuning()
+        self._check(self._L.hc_ens_autotune(self._h, C.byref(t)))
+        return t.as_dict()
 
     def info(self) -> dict:
         s = EnsStats()

@@ -131,3 +131,38 @@ def test_steps_follow_single_system_runs(hc, systems):
         # FP32 forces (relative error ~1e-6) over 4 steps of 1/256
         assert dx < 1e-6, (s, COUNTS[s], dx)
     ens.close()
+
+
+def test_autotune_keeps_the_state_and_the_physics(hc, systems):
+    """hc_ens_autotune times walk-group and direct-sum block candidates on the
+    current bodies without moving them; stepping afterwards gives the same
+    trajectory as an untuned ensemble to the tree walk's FP32 level, and any
+    tuning keeps the direct-sum systems' forces bit for bit."""
+    m, ph = _concat(systems)
+    runs = []
+    for tune in (False, True):
+        ens = hc.Ensemble(COUNTS, tol=TOL, eps=EPS, direct_max=1024)
+        ens.upload(m, ph)
+        ens.step(DT, 0)
+        if tune:
+            before = ens.download()
+            best = ens.autotune()
+            assert best["group_max"] in (32, 48, 64) and best["list_depth"] in (32, 48, 64)
+            assert best["direct_threads"] in (128, 256, 512)
+            assert best["tree_ms"] > 0 and best["direct_ms"] > 0
+            assert ens.tuning()["direct_threads"] == best["direct_threads"]
+            after = ens.download()
+            for x, y in zip(before, after):                 # nothing moved, forces as they were
+                assert np.array_equal(x, y)
+        for k in range(1, 4):
+            ens.step(DT, k)
+        runs.append(ens.download())
+        ens.close()
+    (p0, a0, f0), (p1, a1, f1) = runs
+    np.testing.assert_allclose(p1, p0, rtol=0, atol=1e-6)
+    rel = np.linalg.norm(a1 - a0, axis=1) / np.linalg.norm(a0, axis=1)
+    assert np.percentile(rel, 99.9) < 1e-4
+    ens = hc.Ensemble(COUNTS, tol=TOL, eps=EPS, direct_max=1024)
+    with pytest.raises(hc.HCError):
+        ens.set_tuning(64, 64, 200)
+    ens.close()
