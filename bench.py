@@ -975,9 +975,9 @@ def main():
     ap.add_argument("--train-theta", type=float, default=0.0,
                     help="learned criterion: error budget of the label walk (default: the error rule's equal-RMS budget)")
     ap.add_argument("--train-band", type=float, nargs=2, default=[1.0, 16.0],
-                    help="learned criterion: proxy band (x budget) sampled for training")
+                    help="learned criterion: band lo hi sampled for training, -lo <= log2(proxy/budget) <= hi")
     ap.add_argument("--band", type=float, nargs=2, default=[0.5, 16.0],
-                    help="learned criterion: proxy band (x budget) the network decides in the walk")
+                    help="learned criterion: band lo hi the network decides, -lo <= log2(proxy/budget) <= hi")
     ap.add_argument("--generator", default="host", choices=["host", "device"],
                     help="galaxy workload: draw the bodies with mkgalaxy on the host or hc_generate on the device")
     args = ap.parse_args()
