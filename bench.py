@@ -390,6 +390,25 @@ def timed(ctx, mode, steps, warmup, flush, world):
             "walk_ms": statistics.mean(walk_ms), "launches": launches, "n2b": int(d.n2b), "nbc": int(d.nbc)}
 
 
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) of the GB300s, else the fallback."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
+
+
+def build_bytes(n, nmassive, ncell, usequad=USEQUAD):
+    """Algorithmic bytes of one octree build, each array moved once: keys (24 B of
+    positions read, 16 B of key and index written per body), the sort (16 B per
+    body read and written once), the cell linking (16 B per massive key read),
+    the upward pass (every node's record read once as a child, every cell's
+    record written once: 48 B monopole, 96 B with the quadrupole)."""
+    rec = 96 if usequad else 48
+    return n * (24 + 16) + n * 32 + nmassive * 16 + (nmassive + ncell) * rec + ncell * rec
+
+
 def walk_flops(n2b, nbc):
     return FLOPS_MONO * n2b + (FLOPS_QUAD if USEQUAD else FLOPS_MONO) * nbc
 
@@ -523,6 +542,16 @@ def run_ours(args, world, rank, local):
                 traffic = t.get("learned" if head_mode[0] == "learned" else "body")
         except (OSError, ValueError):
             traffic = None
+    # the octree build against HBM bandwidth (fixed-theta step: no guard beside it)
+    ti = ctx.tree_info()
+    bpk, bsrc = hbm_peak()
+    bbytes = build_bytes(n, int(ti.nbody_massive), int(ti.ncell))
+    b_ms = comp["fixed_theta_0.5"]["build_ms"]
+    roofline_build = {"bound": "hbm", "achieved": bbytes / (b_ms * 1e-3) / 1e9, "peak": bpk, "unit": "GB/s",
+                      "frac": bbytes / (b_ms * 1e-3) / 1e9 / bpk, "algorithmic_bytes": bbytes, "build_ms": b_ms,
+                      "peak_source": bsrc,
+                      "what": "keys + radix sort + cell linking + upward pass, each array moved once; the build "
+                              "is bound by per-level latency, not bandwidth"}
     # body slots per list entry: 32 lanes, two bodies each under the group criteria
     slots = 32 if head_mode[0] == "body" else 64
     ws["mask_fill"] = (head["n2b"] + head["nbc"]) / max(1, slots * (ws["entries_body"] + ws["entries_cell"]))
@@ -542,6 +571,7 @@ def run_ours(args, world, rank, local):
                      "frac": achieved / peak, "traffic": traffic, "kernel": "k_walk<quad> (headline criterion)",
                      "peak_source": "measured live: FP32 FMA chain kernel (hc_fp32_peak), FMA = 2 flops",
                      "flops_per_launch": flops},
+        "roofline_build": roofline_build,
         "ratios": ratios,
         "headline": {"mode": list(head_mode), "rms": head_err[0], "p99": head_err[1],
                      "target_rms": target, "guard": guard, "build_ms": head["build_ms"],
