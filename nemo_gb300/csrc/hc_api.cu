@@ -135,8 +135,8 @@ int alloc_all(hc_ctx *c)
     HC_TRY(dalloc(c, &c->ncy, mn));
     HC_TRY(dalloc(c, &c->ncz, mn));
     HC_TRY(dalloc(c, &c->flags, 4 * n + 8));
-    HC_TRY(dalloc(c, &c->scan_tmp, 1024));
     const int64_t big = std::max<int64_t>(n, mn);
+    HC_TRY(dalloc(c, &c->scan_tmp, hc_scan_scratch_words(big + 1)));
     HC_TRY(dalloc(c, &c->hist, hc_sort_scratch_words(big)));
     HC_TRY(dalloc(c, &c->cand, n));
     HC_TRY(dalloc(c, &c->ncand, 4));
@@ -290,13 +290,18 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
     c->group_max = HC_GROUP2;
     c->list_depth = 64;
     *out = c;
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // The evaluation's stream has the highest priority and the side stream
+    // (the guard's direct sum beside the build) the lowest: when both have
+    // blocks waiting for an SM, the build's go first.
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
         c->err = "cudaStreamCreate failed";
         return HC_ERR_CUDA;
     }
     for (auto &e : c->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return HC_ERR_CUDA;
-    if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         c->err = "cudaStreamCreate / cudaEventCreate failed";
@@ -314,6 +319,7 @@ int hc_create(hc_ctx **out, int64_t nbody, const hc_params *params)
     HC_CUDA(cudaMemcpy(c->box, &b, sizeof b, cudaMemcpyHostToDevice));
     HC_CUDA(cudaMemset(c->st, 0, 2 * sizeof(hc_status)));
     HC_CUDA(cudaMallocHost((void **)&c->h_diag, 64 * sizeof(double)));
+    HC_TRY(hc_guard_setup(c));
     int r2 = hc_tree_setup(c);
     return r2 != HC_OK ? r2 : hc_walk_setup(c);
 }
@@ -698,7 +704,8 @@ static int launch_evaluation(hc_ctx_ext *c, int slot, double kick_dthf, int64_t 
             c->err = std::string("stream capture: ") + cudaGetErrorString(e);
             return HC_ERR_CUDA;
         }
-        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        // kernel nodes keep the priorities of the streams they were captured on
+        e = cudaGraphInstantiate(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
             g.exec = nullptr;

@@ -217,10 +217,14 @@ __global__ void __launch_bounds__(512) k_ens_direct(const int32_t *dsys, const i
     const double cx = px[b0], cy = py[b0], cz = pz[b0];
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
         const double dx = px[b0 + j] - cx, dy = py[b0 + j] - cy, dz = pz[b0 + j] - cz;
-        const float hx = __double2float_rn(dx), hy = __double2float_rn(dy), hz = __double2float_rn(dz);
-        H[j] = make_float4(hx, hy, hz, __double2float_rn(mass[b0 + j]));
-        L[j] = make_float4(__double2float_rn(dx - (double)hx), __double2float_rn(dy - (double)hy),
-                           __double2float_rn(dz - (double)hz), 0.f);
+        float4 h, l;
+        hc_split_hilo(dx, &h.x, &l.x);          // on the doubles' bits (no FP64-pipe conversions)
+        hc_split_hilo(dy, &h.y, &l.y);
+        hc_split_hilo(dz, &h.z, &l.z);
+        h.w = hc_d2f_rn(mass[b0 + j]);
+        l.w = 0.f;
+        H[j] = h;
+        L[j] = l;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {

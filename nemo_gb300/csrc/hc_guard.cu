@@ -12,9 +12,13 @@
 // ends as if only the fallback walk had run.  No host round trip: the whole
 // sequence is captured in the evaluation's CUDA graph.
 //
-// Direct sum: FP32 with positions split into float hi + lo parts (separations
-// formed as (hi - hi) + (lo - lo)), partial sums per source slice, reduced in
-// FP64 in slice order (deterministic).
+// Direct sum: FP32, partial sums per source slice, reduced in FP64 in slice
+// order (deterministic).  With softening the positions are rounded to FP32:
+// on a Plummer sphere of 2^20 bodies that changes the sampled forces by 3e-8
+// (eps 0.01), 3e-7 (eps 1e-3) and 2e-6 (eps 1e-4) RMS relative, far below any
+// error budget, and a separation is one subtraction.  Without softening close
+// pairs are not bounded by eps: positions are split into float hi + lo parts
+// and separations formed as (hi - hi) + (lo - lo).
 #include "hc_internal.cuh"
 
 namespace {
@@ -25,10 +29,54 @@ constexpr int GT = 256;
 // One thread per sampled body, a block per slice of the sources.  The slice
 // is staged in shared memory in pairs (both bodies' values of one quantity
 // adjacent: the operands of one packed FP32x2 instruction) and summed two
-// sources per step.  With softening the sample's own term is exactly zero (a
-// zero separation); without it (SELF) the sample skips itself explicitly.
-template <bool SELF>
-__global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *mass, const double *px,
+// sources per step.  Softened (eps2 > 0): FP32 positions, 12 packed
+// operations and two rsqrt per pair of sources; the sample's own term is
+// exactly zero (a zero separation).
+__global__ void __launch_bounds__(GT) k_guard_direct_soft(int64_t n, const double *mass, const double *px,
+                                                          const double *py, const double *pz, const int64_t *idx,
+                                                          int ns, float eps2, int64_t slice, float4 *part)
+{
+    __shared__ float4 sp[GT / 2][2];      // (x x' y y') (z z' m m') for two sources
+    const int s = blockIdx.y * GT + threadIdx.x;
+    const bool valid = s < ns;
+    const int64_t me = valid ? idx[s] : -1;
+    const float2 nx = splat2(valid ? -hc_d2f_rn(px[me]) : 0.f), ny = splat2(valid ? -hc_d2f_rn(py[me]) : 0.f),
+                 nz = splat2(valid ? -hc_d2f_rn(pz[me]) : 0.f), e2 = splat2(eps2);
+    const int64_t j0 = (int64_t)blockIdx.x * slice;
+    const int64_t j1 = j0 + slice < n ? j0 + slice : n;
+    float2 ax = splat2(0.f), ay = ax, az = ax;
+    float *f = reinterpret_cast<float *>(sp[threadIdx.x >> 1]) + (threadIdx.x & 1);
+    for (int64_t base = j0; base < j1; base += GT) {
+        const int64_t j = base + threadIdx.x;
+        if (j < j1) {
+            f[0] = hc_d2f_rn(px[j]);
+            f[2] = hc_d2f_rn(py[j]);
+            f[4] = hc_d2f_rn(pz[j]);
+            f[6] = hc_d2f_rn(mass[j]);
+        } else {                                 // pad: massless, far away
+            f[0] = f[2] = f[4] = 1.0e4f;
+            f[6] = 0.f;
+        }
+        __syncthreads();
+        const int cnt = j1 - base < GT ? (int)(j1 - base) : GT;
+        for (int p = 0; p < (cnt + 1) >> 1; p++) {
+            const float4 P = sp[p][0], Q = sp[p][1];
+            const float2 dx = __fadd2_rn(lo2(P), nx), dy = __fadd2_rn(hi2(P), ny), dz = __fadd2_rn(lo2(Q), nz);
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+            const float2 w = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+            const float2 mr3 = __fmul2_rn(hi2(Q), __fmul2_rn(w, __fmul2_rn(w, w)));
+            ax = __ffma2_rn(mr3, dx, ax);
+            ay = __ffma2_rn(mr3, dy, ay);
+            az = __ffma2_rn(mr3, dz, az);
+        }
+        __syncthreads();
+    }
+    if (valid) part[(int64_t)blockIdx.x * ns + s] = make_float4(ax.x + ax.y, ay.x + ay.y, az.x + az.y, 0.f);
+}
+
+// Without softening: positions as hi + lo floats, the sample skips itself
+// explicitly.
+__global__ void __launch_bounds__(GT) k_guard_direct_exact(int64_t n, const double *mass, const double *px,
                                                      const double *py, const double *pz, const int64_t *idx, int ns,
                                                      float eps2, int64_t slice, float4 *part)
 {
@@ -37,9 +85,10 @@ __global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *ma
     const bool valid = s < ns;
     const int64_t me = valid ? idx[s] : -1;
     const double xd = valid ? px[me] : 0.0, yd = valid ? py[me] : 0.0, zd = valid ? pz[me] : 0.0;
-    const float xh = __double2float_rn(xd), yh = __double2float_rn(yd), zh = __double2float_rn(zd);
-    const float xl = __double2float_rn(xd - (double)xh), yl = __double2float_rn(yd - (double)yh),
-                zl = __double2float_rn(zd - (double)zh);
+    float xh, yh, zh, xl, yl, zl;
+    hc_split_hilo(xd, &xh, &xl);
+    hc_split_hilo(yd, &yh, &yl);
+    hc_split_hilo(zd, &zh, &zl);
     const int64_t j0 = (int64_t)blockIdx.x * slice;
     const int64_t j1 = j0 + slice < n ? j0 + slice : n;
     const float2 nxh = splat2(-xh), nyh = splat2(-yh), nzh = splat2(-zh);
@@ -49,22 +98,18 @@ __global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *ma
     for (int64_t base = j0; base < j1; base += GT) {
         const int64_t j = base + threadIdx.x;
         if (j < j1) {
-            const double x = px[j], y = py[j], z = pz[j];
-            const float h0 = __double2float_rn(x), h1 = __double2float_rn(y), h2 = __double2float_rn(z);
-            f[0] = h0;
-            f[2] = h1;
-            f[4] = h2;
-            f[6] = __double2float_rn(mass[j]);
-            f[8] = __double2float_rn(x - (double)h0);
-            f[10] = __double2float_rn(y - (double)h1);
-            f[12] = __double2float_rn(z - (double)h2);
+            // hi + lo parts on the doubles' bits (no FP64-pipe conversions)
+            hc_split_hilo(px[j], &f[0], &f[8]);
+            hc_split_hilo(py[j], &f[2], &f[10]);
+            hc_split_hilo(pz[j], &f[4], &f[12]);
+            f[6] = hc_d2f_rn(mass[j]);
         } else {                                 // pad: massless, far away
             f[0] = f[2] = f[4] = 1.0e4f;
             f[6] = f[8] = f[10] = f[12] = 0.f;
         }
         __syncthreads();
         const int cnt = j1 - base < GT ? (int)(j1 - base) : GT;
-        const int self = SELF ? (int)(me - base) : -1;   // the sample's slot in this tile, if any
+        const int self = (int)(me - base);               // the sample's slot in this tile, if any
         for (int p = 0; p < (cnt + 1) >> 1; p++) {
             const float4 H0 = sp[p][0], H1 = sp[p][1], L0 = sp[p][2], L1 = sp[p][3];
             const float2 dx = __fadd2_rn(__fadd2_rn(lo2(H0), nxh), __fadd2_rn(lo2(L0), nxl));
@@ -72,7 +117,7 @@ __global__ void __launch_bounds__(GT) k_guard_direct(int64_t n, const double *ma
             const float2 dz = __fadd2_rn(__fadd2_rn(lo2(H1), nzh), __fadd2_rn(lo2(L1), nzl));
             const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
             float2 w = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-            if (SELF) w = make_float2(2 * p == self ? 0.f : w.x, 2 * p + 1 == self ? 0.f : w.y);
+            w = make_float2(2 * p == self ? 0.f : w.x, 2 * p + 1 == self ? 0.f : w.y);
             const float2 mr3 = __fmul2_rn(hi2(H1), __fmul2_rn(w, __fmul2_rn(w, w)));
             ax = __ffma2_rn(mr3, dx, ax);
             ay = __ffma2_rn(mr3, dy, ay);
@@ -151,18 +196,38 @@ int hc_guard_slices(hc_ctx *c)
     return 8 * nsm;
 }
 
+// Beside the build the direct sum would take every SM's thread slots and
+// registers for its whole run, and the build's kernels would wait for them.
+// Each guard block therefore reserves shared memory it does not use, so that
+// at most four share an SM; the rest of each SM stays free for the build,
+// whose stream has the higher priority.  Four per SM measured best at
+// N = 2^20 (the build beside the guard: 0.86 ms, against 0.885 ms with eight
+// per SM, 0.87 with three or five, 0.885 with two, 0.78 ms with no guard).
+int hc_guard_setup(hc_ctx *c)
+{
+    int dev = 0, smem_sm = 0;
+    HC_CUDA(cudaGetDevice(&dev));
+    HC_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    cudaFuncAttributes fa;
+    HC_CUDA(cudaFuncGetAttributes(&fa, k_guard_direct_exact));   // the larger static footprint of the two
+    const int per_block = smem_sm / 4 - (int)fa.sharedSizeBytes - 1024;   // 1 KB per block is the system's
+    c->guard_smem = per_block > 0 ? per_block : 0;
+    HC_CUDA(cudaFuncSetAttribute(k_guard_direct_soft, cudaFuncAttributeMaxDynamicSharedMemorySize, c->guard_smem));
+    HC_CUDA(cudaFuncSetAttribute(k_guard_direct_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, c->guard_smem));
+    return HC_OK;
+}
+
 // No CUDA queries here: this runs inside stream capture.
 static int guard_slices_used(const hc_ctx *c, int64_t *slice)
 {
-    const int64_t want = c->guard_narrow ? (c->guard_slices + 15) / 16 : c->guard_slices;
+    const int64_t want = c->guard_slices;
     *slice = (c->n + want - 1) / want;
     if (*slice < 1) *slice = 1;
     return (int)((c->n + *slice - 1) / *slice);
 }
 
-// The direct sum needs only positions and masses: it can run while the tree
-// is built.  Beside the build it runs on a sixteenth of the slices (one block
-// per two SMs), leaving the latency-bound build kernels room.
+// The direct sum needs only positions and masses: it runs on a side stream
+// while the tree is built, in the gaps the latency-bound build kernels leave.
 void hc_guard_direct_launch(hc_ctx *c, cudaStream_t s)
 {
     const int ns = (int)c->guard_n;
@@ -171,11 +236,11 @@ void hc_guard_direct_launch(hc_ctx *c, cudaStream_t s)
     const dim3 grid((unsigned)slices, (unsigned)((ns + GT - 1) / GT));
     const float eps2 = (float)(c->prm.eps * c->prm.eps);
     if (eps2 > 0.f)
-        k_guard_direct<false><<<grid, GT, 0, s>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns, eps2, slice,
-                                                   c->guard_part);
+        k_guard_direct_soft<<<grid, GT, c->guard_smem, s>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns,
+                                                         eps2, slice, c->guard_part);
     else
-        k_guard_direct<true><<<grid, GT, 0, s>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns, eps2, slice,
-                                                  c->guard_part);
+        k_guard_direct_exact<<<grid, GT, c->guard_smem, s>>>(c->n, c->mass, c->px, c->py, c->pz, c->guard_idx, ns,
+                                                          eps2, slice, c->guard_part);
     c->launches++;
 }
 

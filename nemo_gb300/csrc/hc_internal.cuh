@@ -16,6 +16,7 @@
 #include <stdint.h>
 #include <string>
 #include "../../include/hackcode_gpu.h"
+#include "hc_f32split.h"
 
 #define HC_IMAX (1 << 30)     // defs.h:124-128
 #define HC_MAXLEVEL 31        // levels 0..30
@@ -76,7 +77,6 @@ struct hc_ctx {
     cudaStream_t side;        // the guard's direct sum, forked from stream, joined before the upward pass
     cudaEvent_t ev_fork, ev_join;
     bool join_pending;        // the build waits on ev_join before the upward pass
-    bool guard_narrow;        // the guard's direct sum runs beside the build on fewer blocks
     cudaEvent_t ev[6];        // 0-1 build, 2-3 walk, 4-5 user timer
     std::string err;
     bool have_tree, have_forces;
@@ -156,6 +156,7 @@ struct hc_ctx {
     int64_t guard_n;                      // sampled bodies (0: off)
     double guard_rms_max;
     int guard_slices;                     // source slices of the direct sum
+    int guard_smem;                       // dynamic shared memory reserved per guard block (residency)
     int64_t *guard_idx;                   // sampled body indices (ascending)
     float4 *guard_part;                   // [slices][guard_n] partial accelerations
     struct hc_guard_state *guard;
@@ -163,7 +164,7 @@ struct hc_ctx {
 
     // scratch
     int32_t *flags;           // n
-    int32_t *scan_tmp;        // block partials
+    uint32_t *scan_tmp;       // single-pass scan: tile counter and look-back words
     uint32_t *hist;           // radix histograms
     int32_t *cand;            // expandbox candidates (original indices)
     int32_t *ncand;
@@ -184,6 +185,7 @@ struct hc_ctx {
 // ---- host-side launchers implemented in the .cu files ----
 // scan / sort (hc_sort.cu)
 void hc_scan_exclusive_i32(hc_ctx *c, const int32_t *in, int32_t *out, int64_t n, int32_t *total_dev);
+int64_t hc_scan_scratch_words(int64_t n);
 // 32-bit words of sort scratch for sorting n keys (n < 2^30)
 int64_t hc_sort_scratch_words(int64_t n);
 int hc_sort_setup(hc_ctx *c);
@@ -226,6 +228,7 @@ void hc_guard_launch(hc_ctx *c);
 // the guard in two parts: the sampled direct sum (on any stream), then the
 // comparison with the walk's forces and the check (on c->stream)
 void hc_guard_direct_launch(hc_ctx *c, cudaStream_t s);
+int hc_guard_setup(hc_ctx *c);
 void hc_guard_check_launch(hc_ctx *c);
 int hc_fma_peak_impl(hc_ctx *c, double *tflops);
 
@@ -282,6 +285,10 @@ static inline int hc_table_gmax(const hc_ctx *c)
     const int cap = c->criterion == 0 ? HC_GROUP : HC_GROUP2;
     return c->group_max >= 1 && c->group_max <= cap ? c->group_max : cap;
 }
+
+// m != 0.0 on the double's bits (a compare is an FP64-pipe instruction):
+// true for NaN, false for +0 and -0
+__device__ __forceinline__ bool hc_nonzero(double m) { return (hc_dbits(m) << 1) != 0; }
 
 static inline int hc_grid(int64_t n, int block, int cap = 152 * 16)
 {

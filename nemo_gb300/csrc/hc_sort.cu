@@ -13,7 +13,6 @@
 
 namespace {
 
-constexpr int SCAN_BLOCK = 512;
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
@@ -47,72 +46,117 @@ __device__ T block_exclusive_scan(T v, T *sh, T *total)
     return base + x - v;
 }
 
-// Phase 1: per-block sums of contiguous chunks.
-template <typename T>
-__global__ void k_scan_reduce(const T *in, int64_t n, int64_t chunk, T *part)
-{
-    __shared__ T sh[32];
-    int64_t beg = (int64_t)blockIdx.x * chunk, end = min(beg + chunk, n);
-    T s = 0;
-    for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) s += in[i];
-    T tot;
-    block_exclusive_scan<T>(s, sh, &tot);
-    if (threadIdx.x == 0) part[blockIdx.x] = tot;
-}
+// Single-pass exclusive scan with decoupled look-back (Merrill and Garland,
+// 2016): tiles of 4096 values take their index from a counter in launch
+// order, publish their sum, and one warp per tile sums the earlier tiles'
+// published values 32 at a time, back to the first tile that already holds
+// its inclusive prefix.  A tile waits only on tiles that hold their index,
+// so every wait ends; each wait is bounded nonetheless and reports an error.
+// Values and prefixes stay below 2^30 (bodies + cells < 2^30).  Loads and
+// stores go through shared memory (one pad word per 32) so that the global
+// accesses are coalesced and each thread scans 16 consecutive values.
+// In place is allowed: a tile reads its inputs before writing its outputs.
+constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 16, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr uint32_t SC_AGG = 1u << 30, SC_PRE = 2u << 30, SC_VAL = (1u << 30) - 1u;
+constexpr int SC_SPIN = 1 << 20;
 
-// Phase 2: exclusive scan of the block sums (one block, <= SCAN_BLOCK parts).
-template <typename T>
-__global__ void k_scan_parts(T *part, int nparts, T *total)
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t *p)
 {
-    __shared__ T sh[32];
-    T v = threadIdx.x < nparts ? part[threadIdx.x] : T(0);
-    T tot;
-    T ex = block_exclusive_scan<T>(v, sh, &tot);
-    if (threadIdx.x < nparts) part[threadIdx.x] = ex;
-    if (threadIdx.x == 0 && total) *total = tot;
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
-
-// Phase 3: scan each chunk, offset by its block prefix, in steps of
-// blockDim x SCAN_ITEMS elements (each thread scans its consecutive items
-// serially; one block scan per step).  In place is allowed: a thread reads
-// its items before writing them.
-constexpr int SCAN_ITEMS = 8;
-template <typename T>
-__global__ void k_scan_down(const T *in, T *out, int64_t n, int64_t chunk, const T *part)
+__device__ __forceinline__ void st_relaxed_u32(uint32_t *p, uint32_t v)
 {
-    __shared__ T sh[32];
-    int64_t beg = (int64_t)blockIdx.x * chunk, end = min(beg + chunk, n);
-    T carry = part[blockIdx.x];
-    for (int64_t t = beg; t < end; t += (int64_t)blockDim.x * SCAN_ITEMS) {
-        const int64_t i0 = t + (int64_t)threadIdx.x * SCAN_ITEMS;
-        T v[SCAN_ITEMS], s = T(0);
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int scan_pad(int e) { return e + (e >> 5); }
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(const int32_t *in, int32_t *out, int64_t n,
+                                                                uint32_t *status, uint32_t *ctr, int32_t *total,
+                                                                int *err)
+{
+    __shared__ int32_t s[SCAN_TILE + SCAN_TILE / 32];
+    __shared__ int32_t sh[32];
+    __shared__ uint32_t s_tile;
+    __shared__ int32_t s_prefix;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(ctr, 1u);
+    __syncthreads();
+    const int64_t tile = s_tile, base = tile * SCAN_TILE;
+    const int tn = (int)(n - base < SCAN_TILE ? n - base : SCAN_TILE);
 #pragma unroll
-        for (int j = 0; j < SCAN_ITEMS; j++) {
-            v[j] = i0 + j < end ? in[i0 + j] : T(0);
-            s += v[j];
-        }
-        T tot;
-        T run = carry + block_exclusive_scan<T>(s, sh, &tot);
-#pragma unroll
-        for (int j = 0; j < SCAN_ITEMS; j++) {
-            if (i0 + j < end) out[i0 + j] = run;
-            run += v[j];
-        }
-        carry += tot;
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const int e = j * SCAN_THREADS + tid;
+        s[scan_pad(e)] = e < tn ? in[base + e] : 0;
     }
+    __syncthreads();
+    int32_t v[SCAN_ITEMS], sum = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        v[j] = s[scan_pad(tid * SCAN_ITEMS + j)];
+        sum += v[j];
+    }
+    int32_t agg;
+    const int32_t excl = block_exclusive_scan<int32_t>(sum, sh, &agg);
+    if (wid == 0) {
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            if (lane == 0) st_relaxed_u32(status, SC_PRE | (uint32_t)agg);
+        } else {
+            if (lane == 0) st_relaxed_u32(status + tile, SC_AGG | (uint32_t)agg);
+            for (int64_t t0 = tile - 1;; t0 -= 32) {
+                const int64_t t = t0 - lane;
+                uint32_t w = SC_PRE;                      // before tile 0: an empty prefix
+                if (t >= 0) {
+                    w = ld_relaxed_u32(status + t);
+                    for (int spin = 0; (w & ~SC_VAL) == 0 && spin < SC_SPIN; spin++) w = ld_relaxed_u32(status + t);
+                    if ((w & ~SC_VAL) == 0) {             // a tile that never published: report, stop
+                        atomicCAS(err, 0, HC_ERR_STATE);
+                        w = SC_PRE;
+                    }
+                }
+                const unsigned pre = __ballot_sync(0xffffffffu, (w & ~SC_VAL) == SC_PRE);
+                const int stop = pre ? __ffs(pre) - 1 : 31;
+                uint32_t x = lane <= stop ? (w & SC_VAL) : 0u;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                prefix += x;
+                if (pre) break;
+            }
+            if (lane == 0) st_relaxed_u32(status + tile, SC_PRE | (prefix + (uint32_t)agg));
+        }
+        if (lane == 0) s_prefix = (int32_t)prefix;
+    }
+    __syncthreads();
+    int32_t run = s_prefix + excl;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        s[scan_pad(tid * SCAN_ITEMS + j)] = run;
+        run += v[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const int e = j * SCAN_THREADS + tid;
+        if (e < tn) out[base + e] = s[scan_pad(e)];
+    }
+    if (total && tid == 0 && base + SCAN_TILE >= n) *total = s_prefix + agg;   // the last tile
 }
 
+// scratch: [0] tile counter, [32, 32 + ntiles) look-back words
 template <typename T>
-void scan_exclusive(cudaStream_t s, const T *in, T *out, int64_t n, T *part, T *total_dev, int64_t *launches)
+void scan_exclusive(cudaStream_t s, const T *in, T *out, int64_t n, uint32_t *scratch, T *total_dev, int *err,
+                    int64_t *launches)
 {
-    int64_t np = (n + 4095) / 4096;
-    int nparts = (int)(np < 1 ? 1 : (np > SCAN_BLOCK ? SCAN_BLOCK : np));
-    int64_t chunk = (n + nparts - 1) / nparts;
-    if (chunk < 1) chunk = 1;
-    k_scan_reduce<T><<<nparts, 256, 0, s>>>(in, n, chunk, part);
-    k_scan_parts<T><<<1, SCAN_BLOCK, 0, s>>>(part, nparts, total_dev);
-    k_scan_down<T><<<nparts, 256, 0, s>>>(in, out, n, chunk, part);
-    *launches += 3;
+    if (n <= 0) {
+        if (total_dev) cudaMemsetAsync(total_dev, 0, sizeof(T), s);
+        return;
+    }
+    const int64_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * (32 + ntiles), s);
+    k_scan_onepass<<<(unsigned)ntiles, SCAN_THREADS, 0, s>>>(in, out, n, scratch + 32, scratch, total_dev, err);
+    *launches += 1;
 }
 
 // ---- radix sort passes over the 64-bit high key ----
@@ -326,8 +370,10 @@ __global__ void k_tie_fix(unsigned long long *hi, uint32_t *lo, uint32_t *val, i
 
 void hc_scan_exclusive_i32(hc_ctx *c, const int32_t *in, int32_t *out, int64_t n, int32_t *total_dev)
 {
-    scan_exclusive<int32_t>(c->stream, in, out, n, c->scan_tmp, total_dev, &c->launches);
+    scan_exclusive<int32_t>(c->stream, in, out, n, c->scan_tmp, total_dev, &c->st->error, &c->launches);
 }
+
+int64_t hc_scan_scratch_words(int64_t n) { return 32 + (n + SCAN_TILE - 1) / SCAN_TILE; }
 
 // Sort (khi, klo, kval)[sel] by the high key bits [begin_bit, end_bit) in
 // 8-bit passes, then order equal-high-key runs by the low key when tie_fix.

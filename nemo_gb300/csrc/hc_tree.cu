@@ -81,19 +81,43 @@ __device__ __forceinline__ bool approx_f32(double x, float *f)
     return true;
 }
 
-// Massive flags, and whether a massive body lies outside the box (intcoord's
-// test, load.c:135-156).  A body clearly inside by an FP32 estimate with a
-// margin far above its error skips the exact FP64 test (the FP64 pipe runs at
-// about 1/60 of the FP32 rate); the rest take it.
-__global__ void k_box_flags(const double *mass, const double *px, const double *py, const double *pz,
-                            int64_t n, const hc_box *box, int32_t *outside, int32_t *massive)
+// the two smallest of two pairs of ascending body indices (INT_MAX: none)
+__device__ __forceinline__ int2 min2(int2 a, int2 b)
 {
+    return make_int2(min(a.x, b.x), min(max(a.x, b.x), min(a.y, b.y)));
+}
+
+__device__ __forceinline__ int2 warp_min2(int2 v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const int2 w = make_int2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+        v = min2(v, w);
+    }
+    return v;
+}
+
+// Whether a massive body lies outside the box (intcoord's test,
+// load.c:135-156), and each block's first two massive bodies in body order
+// (the expansion replay needs the first two of all).  A body clearly inside
+// by an FP32 estimate with a margin far above its error skips the exact FP64
+// test (the FP64 pipe runs at a small fraction of the FP32 rate); the rest
+// take it.
+__global__ void __launch_bounds__(256) k_box_flags(const double *mass, const double *px, const double *py,
+                                                   const double *pz, int64_t n, const hc_box *box, int32_t *outside,
+                                                   int2 *first2)
+{
+    __shared__ int2 wf[8];
     double rmin[3] = {box->rmin[0], box->rmin[1], box->rmin[2]};
     double rsize = box->rsize;
-    const float lo[3] = {(float)rmin[0], (float)rmin[1], (float)rmin[2]}, sz = (float)rsize;
+    const float lo[3] = {hc_d2f_rn(rmin[0]), hc_d2f_rn(rmin[1]), hc_d2f_rn(rmin[2])}, sz = hc_d2f_rn(rsize);
+    int2 f2 = make_int2(INT_MAX, INT_MAX);     // this thread's first two massive bodies (ascending i)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        bool m = mass[i] != 0.0;
-        massive[i] = m;
+        const bool m = hc_nonzero(mass[i]);
+        if (m && f2.y == INT_MAX) {
+            if (f2.x == INT_MAX) f2.x = (int)i;
+            else f2.y = (int)i;
+        }
         const double x[3] = {px[i], py[i], pz[i]};
         bool clear = true;
 #pragma unroll
@@ -108,6 +132,13 @@ __global__ void k_box_flags(const double *mass, const double *px, const double *
         }
         outside[i] = m && !(clear || inbox(x[0], x[1], x[2], rmin, rsize));
     }
+    f2 = warp_min2(f2);
+    if ((threadIdx.x & 31) == 0) wf[threadIdx.x >> 5] = f2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) f2 = min2(f2, wf[w]);
+        first2[blockIdx.x] = f2;
+    }
 }
 
 __global__ void k_box_compact(const int32_t *outside, const int32_t *opos, int64_t n, int32_t *cand)
@@ -120,13 +151,31 @@ __global__ void k_box_compact(const int32_t *outside, const int32_t *opos, int64
 // the start, in body order.  The box only grows, so a body inside stays
 // inside; each round finds the first remaining body outside, expands for
 // it, and continues after it.
-__global__ void k_box_replay(const double *px, const double *py, const double *pz, const int32_t *cand,
-                             const int32_t *ncand_p, const int32_t *mrank, hc_box *box, hc_status *st)
+// The first two massive bodies come from k_box_flags' per-block pairs: the
+// first one (original order) is where the expansion-chain cells hang, the
+// second is the body whose insertion may graft them.
+__global__ void __launch_bounds__(256) k_box_replay(const double *px, const double *py, const double *pz,
+                                                    const int32_t *cand, const int32_t *ncand_p, const int2 *first2,
+                                                    int nblk, hc_box *box, hc_status *st)
 {
     __shared__ int first;
     __shared__ double rmin[3], rsize;
     __shared__ int doublings, chain_before, chain_k;
+    __shared__ int2 wf[8];
+    __shared__ int second_massive;
     const int ncand = *ncand_p;
+    {
+        int2 f2 = make_int2(INT_MAX, INT_MAX);
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x) f2 = min2(f2, first2[b]);
+        f2 = warp_min2(f2);
+        if ((threadIdx.x & 31) == 0) wf[threadIdx.x >> 5] = f2;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); w++) f2 = min2(f2, wf[w]);
+            box->first_massive = f2.x == INT_MAX ? -1 : f2.x;
+            second_massive = f2.y == INT_MAX ? -1 : f2.y;
+        }
+    }
     if (threadIdx.x == 0) {
         rmin[0] = box->rmin[0];
         rmin[1] = box->rmin[1];
@@ -170,7 +219,7 @@ __global__ void k_box_replay(const double *px, const double *py, const double *p
                 rsize = dmul(2.0, rsize);
                 k++;
             }
-            if (mrank[b] == 1 && k >= 2) {   // grafted over a lone first body
+            if (b == second_massive && k >= 2) {   // grafted over a lone first body
                 chain_before = doublings;
                 chain_k = k;
             }
@@ -205,13 +254,6 @@ __global__ void k_box_replay(const double *px, const double *py, const double *p
     }
 }
 
-// first massive body (original order) for the expansion-chain cells
-__global__ void k_first_massive(const int32_t *massive, const int32_t *mrank, int64_t n, hc_box *box)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        if (massive[i] && mrank[i] == 0) box->first_massive = (int)i;
-}
-
 // ---------------- keys ----------------
 
 __device__ __forceinline__ unsigned long long spread21(unsigned v)
@@ -243,13 +285,45 @@ __device__ __forceinline__ int intcoord_clamped(double x, double rmin, double rs
     return xsc < 0.0 ? 0 : HC_IMAX - 1;   // massless bodies / test points outside the box
 }
 
+// intcoord_clamped for a box of size 2^E, with one FP64 operation.  With a
+// power-of-two size the reference's only rounding step is d = x - rmin (the
+// scaling by 2^-E and by IMAX = 2^30 is exact), so
+// floor(IMAX (x - rmin) / rsize) is d's significand shifted right by
+// 22 + E - exponent(d), and 0 <= xsc < 1 reads off d's sign and exponent.
+// Outside the box: 0 below it (negative d), IMAX - 1 above it and for NaN.
+__device__ __forceinline__ int intcoord_pow2(double x, double rmin, int E)
+{
+    const long long b = __double_as_longlong(dsub(x, rmin));
+    const int ef = (int)((b >> 52) & 0x7ff);
+    const long long frac = b & 0xfffffffffffffll;
+    if (ef == 0x7ff) return frac ? HC_IMAX - 1 : (b < 0 ? 0 : HC_IMAX - 1);   // NaN, -inf, +inf
+    if (b < 0) return 0;                    // negative, or -0.0 (inside, cell 0)
+    const int ex = ef ? ef - 1023 : -1022;  // d = sig * 2^(ex - 52)
+    if (ex >= E) return HC_IMAX - 1;        // d >= 2^E: xsc >= 1
+    const long long sig = ef ? (frac | (1ll << 52)) : frac;
+    const int s = 22 + E - ex;              // > 22
+    return s >= 64 ? 0 : (int)(sig >> s);
+}
+
 __global__ void k_keys(const double *x, const double *y, const double *z, int64_t n, const hc_box *box,
                        unsigned long long *khi, uint32_t *klo, uint32_t *kval)
 {
     double r0 = box->rmin[0], r1 = box->rmin[1], r2 = box->rmin[2], rs = box->rsize;
+    // rs = 2^E exactly when its significand bits are zero (a normal double)
+    const uint64_t rb = hc_dbits(rs);
+    const int ref = (int)((rb >> 52) & 0x7ff), E = ref - 1023;
+    const bool pow2 = (rb & 0xfffffffffffffull) == 0 && ref > 0 && ref < 0x7ff && !(rb >> 63);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        unsigned ix = intcoord_clamped(x[i], r0, rs), iy = intcoord_clamped(y[i], r1, rs),
-                 iz = intcoord_clamped(z[i], r2, rs);
+        unsigned ix, iy, iz;
+        if (pow2) {
+            ix = intcoord_pow2(x[i], r0, E);
+            iy = intcoord_pow2(y[i], r1, E);
+            iz = intcoord_pow2(z[i], r2, E);
+        } else {
+            ix = intcoord_clamped(x[i], r0, rs);
+            iy = intcoord_clamped(y[i], r1, rs);
+            iz = intcoord_clamped(z[i], r2, rs);
+        }
         khi[i] = (spread21(ix >> 9) << 2) | (spread21(iy >> 9) << 1) | spread21(iz >> 9);
         klo[i] = (spread9(ix) << 2) | (spread9(iy) << 1) | spread9(iz);
         kval[i] = (uint32_t)i;
@@ -261,7 +335,7 @@ __global__ void k_keys(const double *x, const double *y, const double *z, int64_
 __global__ void k_sorted_massive(const uint32_t *sidx, const double *mass, int64_t n, int32_t *flag)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x)
-        flag[s] = mass[sidx[s]] != 0.0;
+        flag[s] = hc_nonzero(mass[sidx[s]]);
 }
 
 // Massive bodies in key order (tree input) and the walk's target order:
@@ -465,12 +539,8 @@ __global__ void k_children(const int32_t *parent, const uint32_t *bfs2pre, const
     }
 }
 
-__device__ __forceinline__ void split_hilo(double v, float *hi, float *lo)
-{
-    float h = __double2float_rn(v);
-    *hi = h;
-    *lo = __double2float_rn(dsub(v, (double)h));
-}
+// hi = RN_f32(v), lo = RN_f32(v - hi), on the double's bits (no FP64 pipe)
+__device__ __forceinline__ void split_hilo(double v, float *hi, float *lo) { hc_split_hilo(v, hi, lo); }
 
 // Node fields that do not need the upward pass: body leaves (mass and
 // position from the body arrays) and the child range of every cell.
@@ -497,7 +567,7 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
             split_hilo(x, &A.x, &B.x);
             split_hilo(y, &A.y, &B.y);
             split_hilo(z, &A.z, &B.z);
-            A.w = __double2float_rn(m);
+            A.w = hc_d2f_rn(m);
             B.w = -1.0f;
             nodeA[k] = A;
             nodeB[k] = B;
@@ -602,11 +672,19 @@ __global__ void __launch_bounds__(256, 2) k_cofm_all(int usequad, const hc_box *
 {
     cg::grid_group grid = cg::this_grid();
     const int maxd = box->nnode > 0 ? box->max_depth : -1;
+    // A warp takes 32 consecutive cells of a level (one child-count group,
+    // so its FP64 child loop is uniform); consecutive 32-cell chunks go to
+    // consecutive blocks, which sit on different SMs.  A level of a few
+    // thousand cells then spreads over the whole GPU instead of crowding
+    // the FP64 units of the first few SMs.
+    const int nwarps = (int)(grid.size() >> 5);
+    const int wrank = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
+    const int lane = (int)(threadIdx.x & 31);
     for (int D = maxd; D >= 0; D--) {
         // the level's cells only, grouped by child count (coff: group offsets)
         const int ls = (int)coff[D * 8], le = (int)coff[D * 8 + 8];
         const float dsqf = __double2float_rn(box->dsq[D]);
-        for (int j = ls + (int)grid.thread_rank(); j < le; j += (int)grid.size()) {
+        for (int j = ls + wrank * 32 + lane; j < le; j += nwarps * 32) {
             // the cell with its child links in one load (one dependent round trip less)
             const int4 P = cperm[j];
             const int k = P.x, fc = P.y, nc = P.z & 255;
@@ -694,7 +772,7 @@ __global__ void __launch_bounds__(256, 2) k_cofm_all(int usequad, const hc_box *
             ncx[k] = cx;
             ncy[k] = cy;
             ncz[k] = cz;
-            A.w = __double2float_rn(m);
+            A.w = hc_d2f_rn(m);
             B.w = dsqf;
             nodeA[k] = A;
             nodeB[k] = B;
@@ -863,18 +941,15 @@ int hc_tree_build(hc_ctx *c)
     const int B = 256;
     const int G = hc_grid(n, B);
     int32_t *outside = c->flags;
-    int32_t *massive = c->flags + n;
     int32_t *opos = c->flags + 2 * n;
-    int32_t *mrank = c->flags + 3 * n;
+    int2 *first2 = reinterpret_cast<int2 *>(c->flags + 3 * n + (n & 1));   // [G], 8-byte aligned
 
     // 1. expandbox replay
-    k_box_flags<<<G, B, 0, s>>>(c->mass, c->px, c->py, c->pz, n, c->box, outside, massive);
+    k_box_flags<<<G, B, 0, s>>>(c->mass, c->px, c->py, c->pz, n, c->box, outside, first2);
     hc_scan_exclusive_i32(c, outside, opos, n, c->ncand);
-    hc_scan_exclusive_i32(c, massive, mrank, n, nullptr);
     k_box_compact<<<G, B, 0, s>>>(outside, opos, n, c->cand);
-    k_first_massive<<<G, B, 0, s>>>(massive, mrank, n, c->box);
-    k_box_replay<<<1, 256, 0, s>>>(c->px, c->py, c->pz, c->cand, c->ncand, mrank, c->box, c->st);
-    c->launches += 4;
+    k_box_replay<<<1, 256, 0, s>>>(c->px, c->py, c->pz, c->cand, c->ncand, first2, G, c->box, c->st);
+    c->launches += 3;
 
     // 2-3. keys, sort, massive compaction
     hc_keys_for_points(c, c->px, c->py, c->pz, n, c->khi[0], c->klo[0], c->kval[0]);

@@ -113,16 +113,38 @@ def test_forces_at_test_points(hc, quad):
     assert ok.mean() >= FRACTION
 
 
-@pytest.mark.parametrize("kind", ["plummer200003", "cluster60000"])
+def _gridline_positions(n, seed):
+    """Coordinates within a few ulps of the key grid's lines: in the root box
+    (-2, 4) the grid unit is 4 / 2^30 = 2^-28, and x = -2 + k 2^-28 moved by
+    -3..3 ulps puts x - rmin on either side of a line or, rounded, onto it.
+    Each body takes its own random grid cell per axis (no coincident keys)."""
+    rng = np.random.default_rng(seed)
+    k = rng.integers(1, 1 << 30, (n, 3))
+    x = -2.0 + k.astype(np.float64) * 2.0 ** -28
+    for j in range(3):
+        steps = rng.integers(-3, 4, n)
+        for s in range(1, 4):
+            up, dn = steps >= s, steps <= -s
+            x[up, j] = np.nextafter(x[up, j], np.inf)
+            x[dn, j] = np.nextafter(x[dn, j], -np.inf)
+    return x
+
+
+@pytest.mark.parametrize("kind", ["plummer200003", "cluster60000", "gridlines50000"])
 def test_large_tree_bit_exact_vs_oracle(hc, oracle_lib, kind):
     """Trees of many sort tiles (4096 keys each, the last one ragged) against
-    the oracle's maketree/hackcofm: a Plummer sphere of 200,003 bodies, and
+    the oracle's maketree/hackcofm: a Plummer sphere of 200,003 bodies,
     60,000 bodies of which half sit in a cluster of radius 1e-5 (a tree 29
-    levels deep, high key digits shared by half the bodies)."""
+    levels deep, high key digits shared by half the bodies), and 50,000
+    bodies within a few ulps of the key grid's lines (intcoord's rounding of
+    x - rmin decides their cells)."""
     O = oracle_lib
     if kind == "plummer200003":
         m, ph = O.mkplummer(200003, 5)
         pos = ph[:, 0].copy()
+    elif kind == "gridlines50000":
+        pos = _gridline_positions(50000, 23)
+        m = np.full(len(pos), 1.0 / len(pos))
     else:
         rng = np.random.default_rng(17)
         pos = rng.normal(0.0, 1.0, (60000, 3))
