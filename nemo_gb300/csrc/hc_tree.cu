@@ -450,35 +450,6 @@ __global__ void k_emit_preorder(const int32_t *d, const uint32_t *midx, const in
     }
 }
 
-// Last body of each cell: the largest j with lcp(key a, key j) >= level.
-__global__ void k_cell_end(const unsigned long long *mhi, const uint32_t *mlo, const int32_t *d,
-                           const int32_t *pre_depth, const int32_t *pre_a, const hc_box *box, int64_t maxnode,
-                           int32_t *pre_b)
-{
-    const int nn = box->nnode, M = box->nmassive;
-    if (nn > maxnode) return;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nn; p += gridDim.x * blockDim.x) {
-        int a = pre_a[p];
-        if (a < 0) continue;
-        int L = pre_depth[p];
-        if (d[a] < L) {             // one-body expansion cell
-            pre_b[p] = a;
-            continue;
-        }
-        unsigned long long ha = mhi[a];
-        uint32_t la = mlo[a];
-        int step = 1;
-        while (a + step < M && lcp_digits(ha, la, mhi[a + step], mlo[a + step]) >= L) step <<= 1;
-        int lo = a + (step >> 1), hi = min(a + step, M - 1);   // lcp(lo) >= L holds
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (lcp_digits(ha, la, mhi[mid], mlo[mid]) >= L) lo = mid;
-            else hi = mid - 1;
-        }
-        pre_b[p] = lo;
-    }
-}
-
 __global__ void k_levels(const uint32_t *offs, hc_box *box)
 {
     // offs: the depth sort's digit offsets (exclusive scan of its depth counts)
@@ -800,7 +771,10 @@ __global__ void k_set_nmassive(const int32_t *total, hc_box *box) { box->nmassiv
 // at most gmax (<= HC_GROUP) bodies: the cells (and lone bodies) with <= gmax bodies
 // whose parent has more, consecutive siblings packed while they fit.
 
-__device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t *pre_a, const int32_t *pre_b, int k,
+// A node's first massive body (key order) and its body count: the upward
+// pass's count (FP32, exact below 2^24; above it only "more than gmax"
+// matters here).
+__device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t *pre_a, const float4 *nodeQ, int k,
                                           int *first)
 {
     const uint32_t p = bfs2pre[k];
@@ -810,11 +784,11 @@ __device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t
         return 1;
     }
     *first = a;
-    return pre_b[p] - a + 1;
+    return (int)fminf(nodeQ[2 * (int64_t)k + 1].z, 2.0e9f);
 }
 
 template <bool EMIT>
-__global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const int32_t *pre_b, const int32_t *parent,
+__global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const float4 *nodeQ, const int32_t *parent,
                          const int2 *nodeC, const hc_box *box, int64_t maxnode, int gmax, int32_t *ng,
                          const int32_t *goff, int32_t *gstart, int32_t *gcount)
 {
@@ -827,7 +801,7 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const in
             continue;
         }
         int first;
-        const int cnt = node_count(bfs2pre, pre_a, pre_b, k, &first);
+        const int cnt = node_count(bfs2pre, pre_a, nodeQ, k, &first);
         int out = EMIT ? goff[k] : 0, packs = 0;
         if (cnt <= gmax) {                         // only the root can be a small group on its own here
             if (parent[k] < 0) {
@@ -842,7 +816,7 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const in
             int cur = 0, cur_first = 0;
             for (int i = 0; i < nc; i++) {
                 int f;
-                const int cc = node_count(bfs2pre, pre_a, pre_b, fc + i, &f);
+                const int cc = node_count(bfs2pre, pre_a, nodeQ, fc + i, &f);
                 if (cc > gmax || cur + cc > gmax) {
                     if (cur > 0) {
                         if (EMIT) {
@@ -975,8 +949,7 @@ int hc_tree_build(hc_ctx *c)
     const int Gn = hc_grid(c->maxnode, B);
     k_emit_preorder<<<G, B, 0, s>>>(c->dlcp, c->midx, cstart, c->box, c->maxnode, c->pre_info, c->pre_a,
                                     c->dkey[0], c->dval[0]);
-    k_cell_end<<<Gn, B, 0, s>>>(c->mhi, c->mlo, c->dlcp, c->pre_info, c->pre_a, c->box, c->maxnode, c->pre_b);
-    c->launches += 6;
+    c->launches += 5;
 
     // 5. breadth-first layout: stable sort of the pre-order by depth (count on the device)
     uint32_t *nolo[2] = {nullptr, nullptr};
@@ -1023,11 +996,11 @@ int hc_tree_build(hc_ctx *c)
 
     // 7. walk groups aligned with the tree
     const int gmax = hc_table_gmax(c);
-    k_groups<false><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->pre_b, c->parent, c->nodeC,
+    k_groups<false><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->nodeQ, c->parent, c->nodeC,
                                      c->box, c->maxnode, gmax, c->gcnt, nullptr, nullptr, nullptr);
     hc_scan_exclusive_i32(c, c->gcnt, c->goff, c->maxnode + 1, nullptr);
     k_set_ngroups<<<1, 1, 0, s>>>(c->goff, c->maxnode, c->box);
-    k_groups<true><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->pre_b, c->parent, c->nodeC, c->box, c->maxnode,
+    k_groups<true><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->nodeQ, c->parent, c->nodeC, c->box, c->maxnode,
                                     gmax, nullptr, c->goff, c->gstart, c->gcount);
     c->launches += 3;
     return HC_OK;
@@ -1068,7 +1041,20 @@ int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count
     HC_CUDA(cudaMemcpy(bfs2pre, c->bfs2pre, sizeof(uint32_t) * nn, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(pd, c->pre_info, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(pa, c->pre_a, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
-    HC_CUDA(cudaMemcpy(pb, c->pre_b, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
+    // bodies per node, summed up the children links (breadth-first: children
+    // follow their parent, so one pass from the back)
+    {
+        std::unique_ptr<int2[]> C(new int2[nn]);
+        HC_CUDA(cudaMemcpy(C.get(), c->nodeC, sizeof(int2) * nn, cudaMemcpyDeviceToHost));
+        for (int k = nn - 1; k >= 0; k--) {
+            int cnt = 1;
+            if (C[k].x >= 0) {
+                cnt = 0;
+                for (int i = 0; i < (C[k].y & 255); i++) cnt += pb[C[k].x + i];
+            }
+            pb[k] = cnt;
+        }
+    }
     HC_CUDA(cudaMemcpy(mhi, c->mhi, sizeof(unsigned long long) * M, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(mlo, c->mlo, sizeof(uint32_t) * M, cudaMemcpyDeviceToHost));
     HC_CUDA(cudaMemcpy(midx, c->midx, sizeof(uint32_t) * M, cudaMemcpyDeviceToHost));
@@ -1101,7 +1087,7 @@ int hc_tree_dump_impl(hc_ctx *c, int32_t *level, int32_t *corner, int32_t *count
                 corner[3 * ci + ax] = (int32_t)(v & mask);
             }
         }
-        if (count) count[ci] = pb[p] - a + 1;
+        if (count) count[ci] = pb[k];
         if (mass) mass[ci] = nm[k];
         if (cm) {
             cm[3 * ci] = nx[k];
