@@ -291,7 +291,7 @@ def cpu_baseline_one_core(n, m, pos, eps, nsample, seed=0):
 RMS_BUDGET = 1e-3            # the force-error budget of comparison (ii) and of the guard
 GUARD_SAMPLE = 256
 LEARNED_THRESHOLD = 0.0      # logit threshold of the learned criterion (0: the network's own decision)
-BISECT_STEPS = 7
+BISECT_STEPS = 10           # a budget resolution of about 1% over the widest bracket (a factor 2^16)
 
 
 TUNING = {"body": None, "group": {"group_max": 64, "list_depth": 64, "grouping": "tree"}}
