@@ -1,8 +1,9 @@
 """GPU edge cases of the additions: ensembles that are all-direct, all-tree or
 a single system, the rejection of massless ensemble bodies, caller-order
 independence of ensemble results, the approximate criteria and the guard
-without quadrupoles, test points under a group criterion, the guard with
-CUDA graphs off, and more test points than tree nodes between graph replays."""
+without quadrupoles, test points under a group criterion, the guard's direct
+sum against the FP64 one, the guard with CUDA graphs off, and more test points
+than tree nodes between graph replays."""
 import numpy as np
 import pytest
 
@@ -164,6 +165,48 @@ def test_test_points_under_group_criteria(hc):
         r2 = (d ** 2).sum(1) + 0.01 ** 2
         a = (m[:, None] * d / r2[:, None] ** 1.5).sum(0)
         assert np.linalg.norm(ae[j] - a) / np.linalg.norm(a) < 1e-2
+
+
+def _guard_sample(n, nsample, seed):
+    """hc_set_guard's seeded sample: Floyd's algorithm over splitmix64, ascending."""
+    M = (1 << 64) - 1
+    st = (seed * 0x9E3779B97F4A7C15 + 0x632BE59BD9B4E019) & M
+    seen, pick = set(), []
+    for j in range(n - nsample, n):
+        st = (st + 0x9E3779B97F4A7C15) & M
+        z = st
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        z ^= z >> 31
+        t = z % (j + 1)
+        if t in seen:
+            t = j
+        seen.add(t)
+        pick.append(t)
+    return np.array(sorted(pick), dtype=np.int64)
+
+
+@pytest.mark.parametrize("eps", [0.01, 0.0])
+def test_guard_direct_sum_matches_the_fp64_sum(hc, eps):
+    """The guard's RMS error over its sample, from its FP32 direct sum (FP32
+    positions with softening, hi + lo positions without), equals the RMS
+    against the FP64 direct sum of the same bodies to 1e-3 of itself."""
+    n = 65536
+    m, ph = hc.mkplummer(n, 21)
+    ctx = hc.Context(n, tol=0.5, eps=eps, usequad=True)
+    ctx.upload(m, ph)
+    ctx.evaluate()
+    ctx.set_criterion("error", 0.05)
+    ctx.set_guard(256, 1.0, seed=5)
+    ctx.evaluate()
+    _, acc, _ = ctx.download(phase=False, phi=False)
+    idx = _guard_sample(n, 256, 5)
+    ea, _ = ctx.direct_sample(idx)
+    rms = float(np.sqrt(np.mean(_rel(acc[idx], ea) ** 2)))
+    st = ctx.guard_stats()
+    ctx.close()
+    assert st["checks"] == 1 and st["trips"] == 0
+    assert abs(st["last_rms"] - rms) <= 1e-3 * rms + 1e-7, (st["last_rms"], rms)
 
 
 def test_guard_without_graphs(hc):
