@@ -386,8 +386,10 @@ def timed(ctx, mode, steps, warmup, flush, world):
     torch.cuda.synchronize()
     barrier(world)
     d = ctx.diagnostics()
+    ws = ctx.walk_stats()
     return {"step_ms": statistics.mean(step_ms), "build_ms": statistics.mean(build_ms),
-            "walk_ms": statistics.mean(walk_ms), "launches": launches, "n2b": int(d.n2b), "nbc": int(d.nbc)}
+            "walk_ms": statistics.mean(walk_ms), "launches": launches, "n2b": int(d.n2b), "nbc": int(d.nbc),
+            "walk": {k: ws[k] for k in ("candidates", "entries_body", "entries_cell", "network", "network_rounds")}}
 
 
 def hbm_peak():
