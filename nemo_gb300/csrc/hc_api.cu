@@ -64,7 +64,7 @@ void free_all(hc_ctx *c)
 {
     void *ptrs[] = {c->mass, c->px, c->py, c->pz, c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->phi, c->cnt_b,
                     c->cnt_c, c->khi[0], c->khi[1], c->klo[0], c->klo[1], c->kval[0], c->kval[1], c->s_rank,
-                    c->leaf_of_sorted, c->tord, c->gstart, c->gcount, c->gcnt, c->goff, c->mhi, c->mlo, c->midx, c->mpos, c->dlcp, c->ccount, c->pre_info, c->pre_a,
+                    c->leaf_of_sorted, c->tord, c->gstart, c->gcount, c->gcnt, c->goff, c->mhi, c->mlo, c->midx, c->mpos, c->dlcp, c->ccount, c->pre_info, c->pre_a, c->bfs_a,
                     c->dkey[0], c->dkey[1], c->dval[0], c->dval[1], c->pre2bfs, c->parent, c->lastc, c->cperm, c->cbins,
                     c->nodeA, c->nodeB, c->nodeQ, c->nodeC, c->nm, c->ncx, c->ncy, c->ncz, c->flags,
                     c->scan_tmp, c->hist, c->cand, c->ncand, c->diag_part, c->st, c->box, c->tx, c->ty, c->tz,
@@ -114,6 +114,7 @@ int alloc_all(hc_ctx *c)
     const int64_t mn = c->maxnode;
     HC_TRY(dalloc(c, &c->pre_info, mn));
     HC_TRY(dalloc(c, &c->pre_a, mn));
+    HC_TRY(dalloc(c, &c->bfs_a, mn));
     for (int i = 0; i < 2; i++) {
         HC_TRY(dalloc(c, &c->dkey[i], mn));
         HC_TRY(dalloc(c, &c->dval[i], mn));

@@ -112,6 +112,7 @@ struct hc_ctx {
     int64_t maxnode;
     int32_t *pre_info;        // pre-order: level (cell) or -1 (body); bit 31 unused
     int32_t *pre_a;           // pre-order: massive rank of first body
+    uint32_t *bfs_a;          // breadth-first order: pre_a of each node (the depth sort's payload)
     unsigned long long *dkey[2]; // depth sort keys
     uint32_t *dval[2];
     uint32_t *bfs2pre, *pre2bfs;

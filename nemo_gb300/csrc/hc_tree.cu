@@ -476,12 +476,13 @@ __global__ void k_pre2bfs(const uint32_t *bfs2pre, const hc_box *box, uint32_t *
 }
 
 // parent = the node one level up with the largest pre-order index below ours
-__global__ void k_parent(const uint32_t *bfs2pre, const int32_t *pre_depth, const hc_box *box, int32_t *parent)
+// (bdep: each node's depth in breadth-first order, the depth sort's keys)
+__global__ void k_parent(const uint32_t *bfs2pre, const unsigned long long *bdep, const hc_box *box, int32_t *parent)
 {
     const int nn = box->nnode;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
         uint32_t p = bfs2pre[k];
-        int D = pre_depth[p];
+        int D = (int)bdep[k];
         if (D == 0) {
             parent[k] = -1;
             continue;
@@ -496,14 +497,14 @@ __global__ void k_parent(const uint32_t *bfs2pre, const int32_t *pre_depth, cons
     }
 }
 
-__global__ void k_children(const int32_t *parent, const uint32_t *bfs2pre, const int32_t *pre_depth,
-                           const hc_box *box, int2 *nodeC, int32_t *lastc)
+__global__ void k_children(const int32_t *parent, const unsigned long long *bdep, const hc_box *box, int2 *nodeC,
+                           int32_t *lastc)
 {
     const int nn = box->nnode;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
         int p = parent[k];
         if (p < 0) continue;
-        int D = pre_depth[bfs2pre[k]];
+        int D = (int)bdep[k];
         int ls = box->level_start[D], le = box->level_start[D + 1];
         if (k == ls || parent[k - 1] != p) nodeC[p].x = k;
         if (k + 1 == le || parent[k + 1] != p) lastc[p] = k;
@@ -514,9 +515,10 @@ __global__ void k_children(const int32_t *parent, const uint32_t *bfs2pre, const
 __device__ __forceinline__ void split_hilo(double v, float *hi, float *lo) { hc_split_hilo(v, hi, lo); }
 
 // Node fields that do not need the upward pass: body leaves (mass and
-// position from the body arrays) and the child range of every cell.
-__global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, const int32_t *pre_a,
-                            const uint32_t *midx, const uint32_t *mpos, const double *mass, const double *px,
+// position from the body arrays) and the child range of every cell.  bdep,
+// ba: each node's depth and first massive body (-1 - rank for a body leaf)
+// in breadth-first order, carried through the depth sort.
+__global__ void k_node_init(const unsigned long long *bdep, const uint32_t *ba, const uint32_t *midx, const uint32_t *mpos, const double *mass, const double *px,
                             const double *py, const double *pz, const hc_box *box, int2 *nodeC,
                             const int32_t *lastc, float4 *nodeA, float4 *nodeB, float4 *nodeQ, double *nm,
                             double *ncx, double *ncy, double *ncz, int32_t *leaf_of_sorted,
@@ -524,8 +526,7 @@ __global__ void k_node_init(const uint32_t *bfs2pre, const int32_t *pre_depth, c
 {
     const int nn = box->nnode;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
-        uint32_t p = bfs2pre[k];
-        int D = pre_depth[p], a = pre_a[p];
+        int D = (int)bdep[k], a = (int)ba[k];
         if (a < 0) {
             a = -1 - a;
             uint32_t o = midx[a], s = mpos[a];
@@ -774,11 +775,9 @@ __global__ void k_set_nmassive(const int32_t *total, hc_box *box) { box->nmassiv
 // A node's first massive body (key order) and its body count: the upward
 // pass's count (FP32, exact below 2^24; above it only "more than gmax"
 // matters here).
-__device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t *pre_a, const float4 *nodeQ, int k,
-                                          int *first)
+__device__ __forceinline__ int node_count(const uint32_t *ba, const float4 *nodeQ, int k, int *first)
 {
-    const uint32_t p = bfs2pre[k];
-    const int a = pre_a[p];
+    const int a = (int)ba[k];
     if (a < 0) {
         *first = -1 - a;
         return 1;
@@ -788,7 +787,7 @@ __device__ __forceinline__ int node_count(const uint32_t *bfs2pre, const int32_t
 }
 
 template <bool EMIT>
-__global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const float4 *nodeQ, const int32_t *parent,
+__global__ void k_groups(const uint32_t *ba, const float4 *nodeQ, const int32_t *parent,
                          const int2 *nodeC, const hc_box *box, int64_t maxnode, int gmax, int32_t *ng,
                          const int32_t *goff, int32_t *gstart, int32_t *gcount)
 {
@@ -801,7 +800,7 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const fl
             continue;
         }
         int first;
-        const int cnt = node_count(bfs2pre, pre_a, nodeQ, k, &first);
+        const int cnt = node_count(ba, nodeQ, k, &first);
         int out = EMIT ? goff[k] : 0, packs = 0;
         if (cnt <= gmax) {                         // only the root can be a small group on its own here
             if (parent[k] < 0) {
@@ -816,7 +815,7 @@ __global__ void k_groups(const uint32_t *bfs2pre, const int32_t *pre_a, const fl
             int cur = 0, cur_first = 0;
             for (int i = 0; i < nc; i++) {
                 int f;
-                const int cc = node_count(bfs2pre, pre_a, nodeQ, fc + i, &f);
+                const int cc = node_count(ba, nodeQ, fc + i, &f);
                 if (cc > gmax || cur + cc > gmax) {
                     if (cur > 0) {
                         if (EMIT) {
@@ -852,7 +851,7 @@ __global__ void k_set_ngroups(const int32_t *goff, int64_t maxnode, hc_box *box)
 //   bh86: (size/theta)^2;  sw94: (max distance from cm to a corner)^2/theta^2;
 //   "new" (treecode1's default): (size/theta + |cm - centre|)^2;
 //   theta = 0: (2 rsize)^2 (always open).
-__global__ void k_rcrit(int kind, double theta, const hc_box *box, const uint32_t *bfs2pre, const int32_t *pre_a,
+__global__ void k_rcrit(int kind, double theta, const hc_box *box, const uint32_t *ba,
                         const uint32_t *midx, const double *px, const double *py, const double *pz, const int2 *nodeC,
                         const double *ncx, const double *ncy, const double *ncz, float *rcrit2)
 {
@@ -862,7 +861,7 @@ __global__ void k_rcrit(int kind, double theta, const hc_box *box, const uint32_
         const int2 C = nodeC[k];
         if (C.x < 0) continue;                           // body leaf
         const int D = C.y >> 8;
-        const uint32_t o = midx[pre_a[bfs2pre[k]]];
+        const uint32_t o = midx[ba[k]];
         const double p[3] = {px[o], py[o], pz[o]}, cm[3] = {ncx[k], ncy[k], ncz[k]};
         const double size = ldexp(rsize, -D), unit = ldexp(rsize, -30);
         const int shift = 30 - D;
@@ -893,7 +892,7 @@ __global__ void k_rcrit(int kind, double theta, const hc_box *box, const uint32_
 
 void hc_rcrit_launch(hc_ctx *c, int kind, double theta)
 {
-    k_rcrit<<<hc_grid(c->maxnode, 256), 256, 0, c->stream>>>(kind, theta, c->box, c->bfs2pre, c->pre_a, c->midx,
+    k_rcrit<<<hc_grid(c->maxnode, 256), 256, 0, c->stream>>>(kind, theta, c->box, c->bfs_a, c->midx,
                                                               c->px, c->py, c->pz, c->nodeC, c->ncx, c->ncy, c->ncz,
                                                               c->rcrit2);
     c->launches++;
@@ -952,15 +951,22 @@ int hc_tree_build(hc_ctx *c)
     c->launches += 5;
 
     // 5. breadth-first layout: stable sort of the pre-order by depth (count on the device)
-    uint32_t *nolo[2] = {nullptr, nullptr};
-    int dsel = hc_radix_sort_keys(c, c->hist, c->dkey, nolo, c->dval, c->maxnode, 0, 8, false, &c->box->nnode);
+    // the pre-order's first bodies ride along as the sort's low words, so the
+    // later kernels read depth and first body in breadth-first order
+    uint32_t *alo[2] = {reinterpret_cast<uint32_t *>(c->pre_a), c->bfs_a};
+    int dsel = hc_radix_sort_keys(c, c->hist, c->dkey, alo, c->dval, c->maxnode, 0, 8, false, &c->box->nnode);
+    if (dsel != 1) {          // one 8-bit pass: the result is in the second buffers
+        c->err = "depth sort: unexpected pass count";
+        return HC_ERR_STATE;
+    }
     c->bfs2pre = c->dval[dsel];
+    const unsigned long long *bdep = c->dkey[dsel];
     k_levels<<<1, 64, 0, s>>>(c->hist, c->box);      // the sort leaves its digit offsets at hist[0..255]
     k_pre2bfs<<<Gn, B, 0, s>>>(c->bfs2pre, c->box, c->pre2bfs);
-    k_parent<<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_info, c->box, c->parent);
+    k_parent<<<Gn, B, 0, s>>>(c->bfs2pre, bdep, c->box, c->parent);
     k_clear_links<<<Gn, B, 0, s>>>(c->box, c->maxnode, c->nodeC, c->lastc);
-    k_children<<<Gn, B, 0, s>>>(c->parent, c->bfs2pre, c->pre_info, c->box, c->nodeC, c->lastc);
-    k_node_init<<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_info, c->pre_a, c->midx, c->mpos, c->mass, c->px, c->py,
+    k_children<<<Gn, B, 0, s>>>(c->parent, bdep, c->box, c->nodeC, c->lastc);
+    k_node_init<<<Gn, B, 0, s>>>(bdep, c->bfs_a, c->midx, c->mpos, c->mass, c->px, c->py,
                                  c->pz, c->box, c->nodeC, c->lastc, c->nodeA, c->nodeB, c->nodeQ, c->nm, c->ncx,
                                  c->ncy, c->ncz, c->leaf_of_sorted, c->st);
     c->launches += 7;
@@ -996,11 +1002,11 @@ int hc_tree_build(hc_ctx *c)
 
     // 7. walk groups aligned with the tree
     const int gmax = hc_table_gmax(c);
-    k_groups<false><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->nodeQ, c->parent, c->nodeC,
+    k_groups<false><<<Gn, B, 0, s>>>(c->bfs_a, c->nodeQ, c->parent, c->nodeC,
                                      c->box, c->maxnode, gmax, c->gcnt, nullptr, nullptr, nullptr);
     hc_scan_exclusive_i32(c, c->gcnt, c->goff, c->maxnode + 1, nullptr);
     k_set_ngroups<<<1, 1, 0, s>>>(c->goff, c->maxnode, c->box);
-    k_groups<true><<<Gn, B, 0, s>>>(c->bfs2pre, c->pre_a, c->nodeQ, c->parent, c->nodeC, c->box, c->maxnode,
+    k_groups<true><<<Gn, B, 0, s>>>(c->bfs_a, c->nodeQ, c->parent, c->nodeC, c->box, c->maxnode,
                                     gmax, nullptr, c->goff, c->gstart, c->gcount);
     c->launches += 3;
     return HC_OK;
