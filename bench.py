@@ -15,7 +15,11 @@ on a seeded sample of 16,384 bodies.
 
 Prints one JSON line (rank 0).  Under torchrun (N > 1) each rank runs an
 independent replica of the workload on its own GPU (the path does not shard
-across GPUs); the value is the whole-job throughput.
+across GPUs); the value is the whole-job throughput.  A single-GPU default
+run also runs the other configurations briefly in child processes (the
+one-evaluation + 100-step run, the Hernquist sphere, the ensemble, 100 steps
+of the composite galaxy) and summarises their lines under "workloads"
+(--no-cpu-baseline skips them and the CPU baseline).
 """
 from __future__ import annotations
 
@@ -598,8 +602,51 @@ def run_ours(args, world, rank, local):
                                          f"{n} bodies ({tb:.2f} s) + walks of {args.cpu_sample} uniformly sampled "
                                          f"bodies ({rate:.0f} bodies/s), extrapolated to one full evaluation"}
     ctx.close()
+    if world == 1 and rank == 0 and not args.no_cpu_baseline:
+        out["workloads"] = companion_workloads()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+# the other configurations, each a short run of its own workload in a child
+# process (the headline's context is closed first); their lines are
+# summarised under "workloads" so that one default run records all of them
+COMPANIONS = (
+    ("plummer-run", ["--workload", "plummer-run", "--no-cpu-baseline"],
+     ("value", "unit", "ms_per_step", "steps", "ratio_learned_vs_fixed_theta", "rms_error", "clocks")),
+    ("hernquist", ["--workload", "hernquist", "--steps", "5", "--warmup", "2", "--no-cpu-baseline"],
+     ("value", "unit", "ms_per_step", "steps", "ratios", "e2e", "force_error", "clocks")),
+    ("ensemble", ["--workload", "ensemble", "--steps", "5", "--warmup", "2"],
+     ("value", "unit", "ms_per_step", "steps", "phase_ms", "tuning", "energy_drift", "clocks")),
+    ("galaxy", ["--workload", "galaxy", "--generator", "device", "--steps", "100", "--warmup", "2"],
+     ("value", "unit", "ms_per_step", "steps", "evaluation_ms", "rms_error", "energy_drift",
+      "angular_momentum_drift", "guard", "clocks")),
+)
+
+
+def companion_workloads(timeout_s=600):
+    res = {}
+    for name, argv, keys in COMPANIONS:
+        t0 = time.perf_counter()
+        try:
+            p = subprocess.run([sys.executable, os.path.abspath(__file__)] + argv, capture_output=True, text=True,
+                               timeout=timeout_s)
+            lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+            if p.returncode != 0 or not lines:
+                res[name] = {"error": f"exit {p.returncode}: {p.stderr.strip().splitlines()[-1:]}"}
+                continue
+            d = json.loads(lines[-1])
+            res[name] = {k: d[k] for k in keys if k in d}
+            res[name]["metric"] = d.get("metric")
+            if name == "plummer-run":
+                res[name]["runs"] = {k: {"body_steps_per_s": v.get("body_steps_per_s"),
+                                         "energy_drift": v.get("energy_drift"),
+                                         "angular_momentum_drift": v.get("angular_momentum_drift")}
+                                     for k, v in d.get("runs", {}).items()}
+        except subprocess.TimeoutExpired:
+            res[name] = {"error": f"timed out after {timeout_s} s"}
+        res[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+    return res
 
 
 # ---------------------------------------------------------------- config-2 leapfrog run
@@ -996,7 +1043,8 @@ def main():
     ap.add_argument("--sample", type=int, default=16384, help="bodies for the FP64 force-error sample")
     ap.add_argument("--cpu-sample", type=int, default=32768,
                     help="bodies walked by the one-core CPU baseline (about 5-10 s)")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="GPU headline only: no CPU baseline and no companion workload runs")
     ap.add_argument("--no-falcon", action="store_true", help="reference arm: skip the gyrfalcON (falcON) leg")
     ap.add_argument("--workload", default="plummer",
                     choices=["plummer", "plummer-run", "hernquist", "ensemble", "galaxy"],
