@@ -123,7 +123,7 @@ struct hc_ctx {
     int2 *nodeC;
     double *nm, *ncx, *ncy, *ncz;         // FP64 mass and centre of mass per node
     int cofm_grid;                        // co-resident blocks of the upward-pass kernel
-    int walk_blocks[16];                  // resident blocks of each walk variant
+    int walk_blocks[20];                  // resident blocks of each walk variant
     // learned opening criterion: network, training state, samples
     struct MlpSmem *mlp_packed;           // BF16 image used by the walk
     float *mlp_p, *mlp_m, *mlp_v;         // FP32 master weights, Adam moments

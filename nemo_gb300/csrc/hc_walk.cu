@@ -255,9 +255,12 @@ __device__ __forceinline__ void cell_term(const float4 P, const float4 Q0, const
 //         its expansion, m b^p / (dmin - b)^(p+2) (b: radius holding the
 //         cell's bodies; p = 3 with quadrupoles, 2 without), is at most
 //         eps_acc times the group's smallest |a| of the previous evaluation.
-template <bool QUAD, bool COUNT, int MODE>
-// Register budget: 96 (5 blocks of 4 warps per SM) for the per-body rule and
-// the learned walk, 80 (6 blocks) for the group and error rules.
+// COLLECT (learned walk only): the label walk -- analytic decisions, sampled
+// band candidates recorded -- compiled as its own variant, so that the
+// network's walk carries none of its code.
+// Register budget: 96 (5 blocks of 4 warps per SM) for the per-body rule,
+// 128 (4 blocks) for the group, error and learned rules.
+template <bool QUAD, bool COUNT, int MODE, bool COLLECT = false>
 __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs g)
 {
     if (g.run_flag && *g.run_flag == 0) return;   // guard passed: no fallback walk
@@ -688,7 +691,7 @@ __global__ void __launch_bounds__(WARPS * 32, MODE == 0 ? 5 : 4) k_walk(WalkArgs
                         const float budget = g.eps_acc * GUV(13, amin);
                         if (err < budget * g.band_lo_f) accm = my_mask;          // below the band
                         else if (err > budget * g.band_hi_f) openm = my_mask;    // above it
-                        else if (g.collect) {
+                        else if (COLLECT) {
                             // label walk: analytic decision, sampled record of the band candidate
                             const float p_raw = __log2f(fmaxf(err, 1e-38f)) - __log2f(budget);
                             if (err <= budget) accm = my_mask;
@@ -915,21 +918,21 @@ constexpr size_t walk_smem(int mode)
     return sizeof(WarpSmem) * WARPS + (mode == 3 ? sizeof(QueueSmem) * WARPS + sizeof(MlpSmem) : 0);
 }
 
-template <bool Q, bool C, int M>
+template <bool Q, bool C, int M, bool L = false>
 int configure(hc_ctx *c, int variant)
 {
     const size_t smem = walk_smem(M);
-    HC_CUDA(cudaFuncSetAttribute(k_walk<Q, C, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    HC_CUDA(cudaFuncSetAttribute(k_walk<Q, C, M, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, nsm = 0, per_sm = 0;
     HC_CUDA(cudaGetDevice(&dev));
     HC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    HC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<Q, C, M>, WARPS * 32, smem));
+    HC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<Q, C, M, L>, WARPS * 32, smem));
     c->walk_blocks[variant] = nsm * (per_sm < 1 ? 1 : per_sm);
     return HC_OK;
 }
 
 // No CUDA queries here: this runs inside stream capture.
-template <bool Q, bool C, int M>
+template <bool Q, bool C, int M, bool L = false>
 int launch(hc_ctx *c, WalkArgs &a, int variant)
 {
     const size_t smem = walk_smem(M);
@@ -937,7 +940,7 @@ int launch(hc_ctx *c, WalkArgs &a, int variant)
     int64_t need = ((a.ntarget + 31) / 32 + WARPS - 1) / WARPS;
     if (!a.use_table && blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
-    k_walk<Q, C, M><<<(unsigned)blocks, WARPS * 32, smem, c->stream>>>(a);
+    k_walk<Q, C, M, L><<<(unsigned)blocks, WARPS * 32, smem, c->stream>>>(a);
     c->launches++;
     return HC_OK;
 }
@@ -1030,6 +1033,14 @@ int hc_walk_launch(hc_ctx *c, bool self, int64_t ntarget, const uint32_t *tsorte
         a.sample_group = c->sample_group;
         a.sample_node = c->sample_node;
         a.sample_amin = c->sample_amin;
+        if (a.collect) {
+            switch (v) {
+            case 0: return launch<false, false, 3, true>(c, a, 16);
+            case 1: return launch<false, true, 3, true>(c, a, 17);
+            case 2: return launch<true, false, 3, true>(c, a, 18);
+            default: return launch<true, true, 3, true>(c, a, 19);
+            }
+        }
         switch (v) {
         case 0: return launch<false, false, 3>(c, a, 12);
         case 1: return launch<false, true, 3>(c, a, 13);
@@ -1073,6 +1084,10 @@ int hc_walk_setup(hc_ctx *c)
     if (r == HC_OK) r = configure<false, true, 3>(c, 13);
     if (r == HC_OK) r = configure<true, false, 3>(c, 14);
     if (r == HC_OK) r = configure<true, true, 3>(c, 15);
+    if (r == HC_OK) r = configure<false, false, 3, true>(c, 16);
+    if (r == HC_OK) r = configure<false, true, 3, true>(c, 17);
+    if (r == HC_OK) r = configure<true, false, 3, true>(c, 18);
+    if (r == HC_OK) r = configure<true, true, 3, true>(c, 19);
     return r;
 }
 
