@@ -363,7 +363,9 @@ double hc_nemo_eval(const char *expr, int *ok);
  * the external part itself).  The per-block partials use a static device
  * array sized for at most 8,388,608 bodies; larger n returns HC_ERR_ARG.  The
  * first call on a device looks the array up (cudaGetSymbolAddress) and should
- * come before any stream capture; after cudaDeviceReset of a device the
+ * come before any stream capture; with lazy module loading the CUDA driver may
+ * also load the entry point's kernels at that call, which takes device memory
+ * for their code (later calls take none); after cudaDeviceReset of a device the
  * looked-up address is stale and the entry point must not be called on it
  * again.  All calls on a device share the array: calls that overlap on the
  * GPU race and must be serialised by the caller. */

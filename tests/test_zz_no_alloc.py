@@ -5,10 +5,10 @@ runtime that only lends them pre-registered buffers from its own pool, or a
 real-time loop that must not pay cudaMalloc's implicit synchronisation).  The
 entry point takes device pointers to the body arrays and to the result and
 keeps its per-block partials in a static device array.  This test calls it
-through the C ABI twice in a row and checks both results against the regular
-entry point (hc_diagnostics), to the 1e-12 relative tolerance used for FP64
-reductions here, and checks that the device's free memory is the same before
-and after the calls.  It lives in a file of its own that pytest collects last.
+through the C ABI once, then twice in a row, and checks both results against
+the regular entry point (hc_diagnostics), to the 1e-12 relative tolerance used
+for FP64 reductions here, and checks that the device's free memory is the same
+before and after those two calls.  It lives in a file of its own that pytest collects last.
 """
 import ctypes as C
 
@@ -53,6 +53,10 @@ def test_noalloc_diagnostics_match_regular_entry_point():
     out = torch.zeros(36, dtype=torch.float64, device=dev)
     L = hc.library()
     results = []
+    # the first call on the device looks the static array up, and the CUDA
+    # driver may load the entry point's kernels then (lazy loading takes
+    # device memory for their code); the calls measured below follow it
+    assert L.hc_diagnostics_noalloc(n, *[t.data_ptr() for t in tens], out.data_ptr(), None) == 0
     torch.cuda.synchronize()
     free_before, _ = torch.cuda.mem_get_info()           # cudaMemGetInfo
     for _ in range(2):                                   # two calls in a row share the static array
