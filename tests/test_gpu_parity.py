@@ -164,6 +164,32 @@ def test_large_tree_bit_exact_vs_oracle(hc, oracle_lib, kind):
         assert np.array_equal(got[f], ref[f]), f
 
 
+@pytest.mark.parametrize("rsize", [3.0, 4.0])
+def test_box_of_any_size(hc, oracle_lib, rsize):
+    """A root box set by the caller (a restart file carries one): size 3 is
+    no power of two, so intcoord takes its FP64 division (load.c:135-156)
+    rather than the integer path of a power-of-two box; both against the
+    oracle's tree, after expandbox has doubled the box to hold every body."""
+    O = oracle_lib
+    m, ph = O.mkplummer(30011, 31)
+    pos = ph[:, 0].copy()
+    rmin = np.array([-1.5, -1.25, -1.0])
+    T = O.Tree(len(m), 1.0)
+    T.set_box(rmin, rsize)
+    assert T.build(m, pos, True) == 0
+    ref = _canon(T.dump())
+    with hc.Context(len(m), tol=0.6, eps=0.01, fcells=1.0, usequad=True) as ctx:
+        ctx.upload(m, ph)
+        ctx.set_box(rmin, rsize)
+        ctx.build_tree()
+        (grmin, grsize), (ormin, orsize) = ctx.box(), T.box()
+        got = _canon(ctx.dump_tree())
+    assert np.array_equal(grmin, ormin) and grsize == orsize
+    assert len(got["level"]) == len(ref["level"])
+    for f in ("level", "corner", "count", "mass", "cm"):
+        assert np.array_equal(got[f], ref[f]), f
+
+
 def test_expansion_chain_and_massless(hc, oracle_lib):
     """One-body expansion cells (load.c:74-93) and massless test bodies."""
     O = oracle_lib
