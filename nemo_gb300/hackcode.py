@@ -203,7 +203,10 @@ def _ptr(a):
 
 
 class Context:
-    """One system of nbody bodies on the GPU (one CUDA stream, all memory owned)."""
+    """One system of nbody bodies on the GPU, all memory owned.  Its work runs
+    on its own CUDA streams: the evaluation's at the device's highest stream
+    priority, a side stream (the guard's direct sum beside the build) at the
+    lowest."""
 
     def __init__(self, nbody: int, tol: float = 1.0, eps: float = 0.05, fcells: float = 1.0,
                  usequad: bool = False, count_per_body: bool = False):
